@@ -1,0 +1,132 @@
+/*
+ * sdns_gb300.h -- C ABI of the GB300 (sm_103a) backend for the triply
+ * periodic pseudo-spectral Navier-Stokes solver of spectralDNS.
+ *
+ * One context = one grid on one GPU with one CUDA stream.  All entry points
+ * return an int status (SDNS_OK == 0); on failure sdns_last_error() gives a
+ * message.  Nothing traps or exits.  Buffers passed by the caller are either
+ * host memory (where == SDNS_HOST; pinned memory is fastest) or device memory
+ * of the context's GPU (where == SDNS_DEVICE); the call is synchronous with
+ * respect to the caller's buffers when they are host memory.
+ *
+ * Array layouts follow the reference's single-rank numpy arrays (C order):
+ *   spectral vector  (3, N0, N1, N2/2+1) complex  -- U_hat, dU, Source
+ *   physical vector  (3, N0, N1, N2) real         -- U, curl
+ * "complex" is complex64 (SDNS_SINGLE) or complex128 (SDNS_DOUBLE), matching
+ * spectralDNS/solvers/spectralinit.py:25-29 (datatypes).
+ *
+ * Reference interfaces replaced (paths inside the spectralDNS tree):
+ *   sdns_create/sdns_destroy  spectralDNS/solvers/NS.py:12-72   get_context
+ *   sdns_compute_rhs          spectralDNS/solvers/NS.py:219-261 ComputeRHS (Vortex form,
+ *                             NS.py:191-198, with add_pressure_diffusion NS.py:203-217)
+ *   sdns_rk4                  spectralDNS/maths/integrators.py:149-159 RK4 (closure :188-191)
+ *   sdns_forward              shenfun VT.forward as called at NS.py:101-104 (set_velocity)
+ *   sdns_backward             shenfun VT.backward as called at NS.py:91-94  (get_velocity)
+ *   sdns_curl                 spectralDNS/solvers/NS.py:86-89, 124-129 (get_curl / compute_curl)
+ *   sdns_pressure             spectralDNS/solvers/NS.py:96-99  (get_pressure)
+ *   sdns_divergence           spectralDNS/solvers/NS.py:106-110 (get_divergence)
+ *   sdns_set_state/get_state  the U_hat array of the context (NS.py:52, 58)
+ *   sdns_set_source           the Source array added in ComputeRHS (NS.py:63, 259)
+ *   sdns_diagnostics          demo/TG.py:97-103 and demo/Isotropic.py:167, 241-249 reductions
+ *   sdns_spectrum             demo/Isotropic.py:88-114 (shell spectrum, bins k+0.5)
+ */
+#ifndef SDNS_GB300_H
+#define SDNS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SDNS_ABI_VERSION 1
+
+enum sdns_status {
+  SDNS_OK = 0,
+  SDNS_EINVAL = 1,   /* bad argument or unsupported configuration */
+  SDNS_ECUDA = 2,    /* CUDA runtime error */
+  SDNS_ENOMEM = 3,   /* device allocation failed */
+  SDNS_ESTATE = 4,   /* call out of order (e.g. no state set) */
+  SDNS_ENONFINITE = 5 /* a reduction found NaN/Inf in the solution */
+};
+
+enum sdns_precision { SDNS_SINGLE = 0, SDNS_DOUBLE = 1 };
+enum sdns_dealias { SDNS_DEALIAS_23 = 0, SDNS_DEALIAS_NONE = 1 };
+enum sdns_where { SDNS_HOST = 0, SDNS_DEVICE = 1 };
+
+typedef struct sdns_ctx sdns_ctx;
+
+typedef struct sdns_config {
+  int32_t n[3];          /* grid points per axis, powers of two in [16, 1024] */
+  double L[3];           /* box lengths (K scaled by 2 pi / L, NS.py:38) */
+  double nu;             /* viscosity */
+  int32_t precision;     /* SDNS_SINGLE: FP32 transforms, FP64 RK4 accumulators;
+                            SDNS_DOUBLE: everything FP64 */
+  int32_t dealias;       /* SDNS_DEALIAS_23 (|k_i| < 2/3 (N_i/2+1)) or
+                            SDNS_DEALIAS_NONE (Nyquist planes masked) */
+  int32_t device;        /* CUDA device ordinal */
+  int32_t store_pressure;/* keep P_hat of the last RK4 stage for sdns_pressure */
+  int32_t reserved[4];
+} sdns_config;
+
+/* diagnostics written by sdns_diagnostics (float64, full-spectrum sums) */
+enum sdns_diag {
+  SDNS_DIAG_ENERGY = 0,      /* 1/2 <u.u>              (demo/TG.py:98)  */
+  SDNS_DIAG_ENSTROPHY = 1,   /* 1/2 <w.w>              (demo/TG.py:97)  */
+  SDNS_DIAG_DISSIPATION = 2, /* nu * energy_fourier(i K x u_hat) (demo/Isotropic.py:241-249) */
+  SDNS_DIAG_DIVERGENCE = 3,  /* 1/2 <(div u)^2>        (demo/TG.py:102-103) */
+  SDNS_DIAG_CFL_RATE = 4,    /* max |u|/dx+|v|/dy+|w|/dz at the last RK4 step start */
+  SDNS_DIAG_TIME = 5,        /* simulated time accumulated by sdns_rk4 */
+  SDNS_DIAG_LAST_DT = 6,     /* time step of the last RK4 step */
+  SDNS_DIAG_COUNT = 8
+};
+
+int sdns_abi_version(void);
+const char* sdns_last_error(void);
+
+int sdns_create(const sdns_config* cfg, sdns_ctx** out);
+int sdns_destroy(sdns_ctx* ctx);
+int sdns_synchronize(sdns_ctx* ctx);
+/* bytes of device memory held by the context */
+int sdns_memory_bytes(sdns_ctx* ctx, int64_t* bytes);
+
+int sdns_set_state(sdns_ctx* ctx, const void* u_hat, int where);
+int sdns_get_state(sdns_ctx* ctx, void* u_hat, int where);
+/* Source term (NULL clears it); spectral vector layout */
+int sdns_set_source(sdns_ctx* ctx, const void* source, int where);
+
+int sdns_compute_rhs(sdns_ctx* ctx, const void* u_hat, void* rhs, int where);
+
+/* Constant-power forcing on 0 < |K| <= kf (a Source recomputed from the
+ * state at the start of every RK4 step); eps <= 0 switches it off. */
+int sdns_set_forcing(sdns_ctx* ctx, double eps, double kf);
+/* CFL time step dt = cfl / max(|u|/dx+|v|/dy+|w|/dz), evaluated on the
+ * dealiased velocity at the start of each step; cfl <= 0 switches it off. */
+int sdns_set_cfl(sdns_ctx* ctx, double cfl);
+
+/* nsteps classic RK4 steps of size dt (ignored when CFL is on).  The
+ * simulated time is accumulated on the device (SDNS_DIAG_TIME). */
+int sdns_rk4(sdns_ctx* ctx, double dt, int32_t nsteps);
+int sdns_set_time(sdns_ctx* ctx, double t);
+
+/* transforms of nfields (1..3) scalar fields stacked on the first axis */
+int sdns_forward(sdns_ctx* ctx, const void* phys, void* spec, int32_t nfields, int where);
+int sdns_backward(sdns_ctx* ctx, const void* spec, void* phys, int32_t nfields, int where);
+/* physical fields computed from the context state */
+int sdns_velocity(sdns_ctx* ctx, void* u, int where);
+int sdns_curl(sdns_ctx* ctx, void* curl, int where);
+int sdns_pressure(sdns_ctx* ctx, void* p, int where);
+int sdns_divergence(sdns_ctx* ctx, void* div, int where);
+
+int sdns_diagnostics(sdns_ctx* ctx, double* out /* SDNS_DIAG_COUNT */);
+int sdns_spectrum(sdns_ctx* ctx, double* Ek, int32_t nbins);
+
+/* device time (ms) of the kernels of the last sdns_rk4 call, per kernel
+ * class, measured with CUDA events on the context stream when timing is on */
+int sdns_set_timing(sdns_ctx* ctx, int32_t on);
+int sdns_get_timing(sdns_ctx* ctx, double* ms /* 8 */, int32_t* launches /* 8 */);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SDNS_GB300_H */

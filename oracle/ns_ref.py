@@ -1,0 +1,281 @@
+"""CPU oracle for the triply-periodic pseudo-spectral Navier-Stokes RK4 step.
+
+TEST INFRASTRUCTURE ONLY.  This module is the float64 (or float32) NumPy /
+scipy.fft restatement of the spectralDNS NS "Vortex" path that the GPU
+library is checked against.  Only the test-suite, ``__graft_entry__.smoke()``
+and the CPU-baseline leg of ``bench.py`` may import it; the product path
+(``spectraldns_gb300``) never does.
+
+What it restates (paths relative to the spectralDNS source tree):
+
+* ``spectralDNS/solvers/NS.py:12-72``   get_context: wavenumbers ``K`` scaled by
+  ``2*pi/L`` (:38-41), ``K2`` (:42-44), ``K_over_K2`` with ``K2==0 -> 1``
+  (:46-48).
+* ``spectralDNS/solvers/NS.py:124-136, 191-198``  Vortex convection:
+  ``u = F^-1(u_hat)``, ``curl = F^-1(i K x u_hat)``, ``rhs = F(u x curl)``.
+* ``spectralDNS/solvers/NS.py:203-217``  add_pressure_diffusion:
+  ``P_hat = sum(rhs*K_over_K2)``; ``rhs -= P_hat*K``; ``rhs -= nu*K2*u_hat``.
+* ``spectralDNS/solvers/NS.py:219-261``  ComputeRHS (``rhs += Source``, :259).
+* ``spectralDNS/maths/integrators.py:149-159, 185-186``  classic RK4 with
+  ``a=[1/6,1/3,1/3,1/6]``, ``b=[1/2,1/2,1]``.
+* ``spectralDNS3D_short.py:36-46, 76-86`` and ``cpp/spectralDNS.cpp:122-129,
+  217-236``  the explicit 2/3 rule: keep modes with ``|k_i| < (2/3)(N_i/2+1)``
+  on every axis (integer wave index), applied to the nonlinear term on
+  output; NS.py (``dealias_direct``) also truncates the transform input,
+  which this oracle does as well (a no-op when the state is inside the set).
+* Transform conventions of shenfun (third party, not vendored): forward
+  R2C over the last axis, C2C over the others, normalised by 1/(N0 N1 N2);
+  backward unnormalised.  In-tree evidence: ``demo/TG.py:98-109`` (Parseval
+  check ``energy_fourier(U_hat)/2 - 1/2<U^2> ~ 0``) and
+  ``demo/Isotropic.py:67-69``.
+* Diagnostics: ``demo/TG.py:97-103, 116-126`` (float64 mean-square
+  reductions), ``demo/Isotropic.py:88-147`` (shell spectrum).
+
+Build-defined parts (not in the reference, mirrored by the GPU library):
+the seeded ``k^4 exp(-2 (k/k0)^2)`` solenoidal initial field, the
+constant-power low-wavenumber forcing (a ``Source`` recomputed at the start
+of every RK4 step) and the CFL time step.
+
+Parity pins: the Taylor-Green known answers ``k=0.124953117517`` and
+``w=0.375249930801`` (``tests/TG.py:125-126``, ``spectralDNS3D_short.py:113``)
+and state fixtures produced by running ``spectralDNS3D_short.py`` itself
+(``tests/golden/make_golden.py``).
+"""
+from __future__ import annotations
+
+import math
+import numpy as np
+
+try:  # scipy.fft is threaded (workers=); numpy.fft is the fallback
+    import scipy.fft as _fft
+    _HAVE_SCIPY = True
+except ImportError:  # pragma: no cover
+    import numpy.fft as _fft
+    _HAVE_SCIPY = False
+
+RK4_A = (1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0)
+RK4_B = (0.5, 0.5, 1.0)
+
+
+def dealias_cutoff(n: int, rule: str = "2/3-rule") -> int:
+    """Largest kept integer wave index |k| on an axis of n points.
+
+    2/3 rule: keep |k| < (2/3)(n/2+1)  (spectralDNS3D_short.py:44-46).
+    'None' (Nyquist masked): keep |k| <= n/2-1.
+    """
+    if rule == "2/3-rule":
+        kmax = 2.0 / 3.0 * (n // 2 + 1)
+        kc = int(math.ceil(kmax)) - 1
+        while kc + 1 < kmax:
+            kc += 1
+        while kc >= kmax:
+            kc -= 1
+        return kc
+    if rule in ("None", None):
+        return n // 2 - 1
+    raise ValueError("unsupported dealias rule %r" % (rule,))
+
+
+class Grid:
+    """Spectral/physical grid of the triply periodic box (NS.py:12-48)."""
+
+    def __init__(self, N, L=(2 * np.pi,) * 3, nu=0.000625, dealias="2/3-rule",
+                 dtype=np.float64, workers=1):
+        self.N = tuple(int(n) for n in N)
+        self.L = tuple(float(l) for l in L)
+        self.nu = float(nu)
+        self.dealias = dealias
+        self.dtype = np.dtype(dtype)
+        self.cdtype = np.result_type(self.dtype, np.complex64)
+        self.workers = workers
+        n0, n1, n2 = self.N
+        self.spec_shape = (n0, n1, n2 // 2 + 1)
+        # integer wave indices in FFT order; R2C axis 0..n2/2
+        self.ki = [np.fft.fftfreq(n0, 1.0 / n0).astype(np.int64),
+                   np.fft.fftfreq(n1, 1.0 / n1).astype(np.int64),
+                   np.arange(n2 // 2 + 1, dtype=np.int64)]
+        # Nyquist index of the complex axes is -n/2 (fftfreq); the R2C
+        # Nyquist +n2/2 is outside every kept set.
+        scale = [2 * np.pi / l for l in self.L]
+        k1d = [self.ki[i].astype(np.float64) * scale[i] for i in range(3)]
+        self.K = [k1d[0][:, None, None], k1d[1][None, :, None], k1d[2][None, None, :]]
+        self.K2 = self.K[0] ** 2 + self.K[1] ** 2 + self.K[2] ** 2
+        K2n = np.where(self.K2 == 0, 1.0, self.K2)
+        self.K_over_K2 = [self.K[i] / K2n for i in range(3)]
+        self.kc = [dealias_cutoff(n, dealias) for n in self.N]
+        m0 = np.abs(self.ki[0]) <= self.kc[0]
+        m1 = np.abs(self.ki[1]) <= self.kc[1]
+        m2 = np.abs(self.ki[2]) <= self.kc[2]
+        self.mask = (m0[:, None, None] & m1[None, :, None] & m2[None, None, :])
+        # the physical mesh (NS.py:37 via shenfun local_mesh)
+        self.X = [(np.arange(self.N[i]) * self.L[i] / self.N[i]) for i in range(3)]
+
+    # --- transforms (shenfun conventions) --------------------------------
+    def forward(self, u):
+        """R2C over the last axis, C2C over the others, scaled by 1/prod(N)."""
+        kw = {"workers": self.workers} if _HAVE_SCIPY else {}
+        out = _fft.rfftn(u, axes=(-3, -2, -1), **kw) / float(np.prod(self.N))
+        return out.astype(self.cdtype, copy=False)
+
+    def backward(self, uh):
+        """Unnormalised inverse (C2C, C2C, C2R)."""
+        kw = {"workers": self.workers} if _HAVE_SCIPY else {}
+        out = _fft.irfftn(uh, s=self.N, axes=(-3, -2, -1), **kw) * float(np.prod(self.N))
+        return out.astype(self.dtype, copy=False)
+
+    # --- pieces of ComputeRHS --------------------------------------------
+    def curl_hat(self, uh):
+        """cross2: i K x u_hat (maths/cross.py:27-32)."""
+        K = self.K
+        c = np.empty_like(uh)
+        c[0] = 1j * (K[1] * uh[2] - K[2] * uh[1])
+        c[1] = 1j * (K[2] * uh[0] - K[0] * uh[2])
+        c[2] = 1j * (K[0] * uh[1] - K[1] * uh[0])
+        return c
+
+    @staticmethod
+    def cross(a, b):
+        """cross1: a x b for real fields (maths/cross.py:13-25)."""
+        c = np.empty_like(a)
+        c[0] = a[1] * b[2] - a[2] * b[1]
+        c[1] = a[2] * b[0] - a[0] * b[2]
+        c[2] = a[0] * b[1] - a[1] * b[0]
+        return c
+
+    def compute_rhs(self, uh, source=None, return_parts=False):
+        """ComputeRHS for the Vortex form (NS.py:219-261)."""
+        m = self.mask
+        uhm = uh * m
+        u = self.backward(uhm)
+        w = self.backward(self.curl_hat(uhm))
+        nl = self.forward(self.cross(u, w)) * m
+        P = nl[0] * self.K_over_K2[0] + nl[1] * self.K_over_K2[1] + nl[2] * self.K_over_K2[2]
+        rhs = np.empty_like(uh)
+        for i in range(3):
+            rhs[i] = nl[i] - P * self.K[i] - self.nu * self.K2 * uh[i]
+        if source is not None:
+            rhs += source
+        if return_parts:
+            return rhs, dict(u=u, curl=w, nl=nl, P_hat=P)
+        return rhs
+
+    def rk4_step(self, uh, dt, source=None):
+        """One classic RK4 step (integrators.py:149-159)."""
+        u0 = uh.copy()
+        u1 = uh.copy()
+        u2 = uh.copy()
+        dtc = np.asarray(dt, dtype=self.dtype)
+        for rk in range(4):
+            rhs = self.compute_rhs(u0, source)
+            if rk < 3:
+                u0 = u1 + np.asarray(RK4_B[rk], self.dtype) * dtc * rhs
+            u2 += np.asarray(RK4_A[rk], self.dtype) * dtc * rhs
+        return u2
+
+    # --- diagnostics ------------------------------------------------------
+    def hermitian_weights(self):
+        n2 = self.N[2]
+        w = np.full(self.spec_shape[2], 2.0)
+        w[0] = 1.0
+        if n2 % 2 == 0:
+            w[-1] = 1.0
+        return w
+
+    def energy_fourier(self, uh):
+        """sum over the full spectrum of |u_hat|^2 = <u.u> (shenfun energy_fourier)."""
+        w = self.hermitian_weights()
+        return float(np.sum((np.abs(uh.astype(np.complex128)) ** 2) * w))
+
+    def mean_square(self, f):
+        """sum(f*f)/prod(N) in float64 (demo/TG.py:97-98)."""
+        f = f.astype(np.float64)
+        return float(np.sum(f * f) / np.prod(self.N))
+
+    def kinetic_energy(self, uh):
+        return 0.5 * self.mean_square(self.backward(uh))
+
+    def enstrophy(self, uh):
+        return 0.5 * self.mean_square(self.backward(self.curl_hat(uh)))
+
+    def divergence_ms(self, uh):
+        K = self.K
+        d = 1j * (K[0] * uh[0] + K[1] * uh[1] + K[2] * uh[2])
+        return 0.5 * self.mean_square(self.backward(d)[None])
+
+    def dissipation(self, uh):
+        """nu * energy_fourier(i K x u_hat) (demo/Isotropic.py:241-249)."""
+        return self.nu * self.energy_fourier(self.curl_hat(uh))
+
+    def spectrum(self, uh):
+        """Shell spectrum of demo/Isotropic.py:88-114 (bins at k+0.5)."""
+        uiui = np.zeros(uh[0].shape)
+        uiui[..., 1:-1] = 2 * np.sum((uh[..., 1:-1] * np.conj(uh[..., 1:-1])).real, axis=0)
+        uiui[..., 0] = np.sum((uh[..., 0] * np.conj(uh[..., 0])).real, axis=0)
+        uiui[..., -1] = np.sum((uh[..., -1] * np.conj(uh[..., -1])).real, axis=0)
+        uiui *= (4.0 / 3.0 * np.pi)
+        Nb = int(np.sqrt(np.sum((np.array(self.N) / 2) ** 2) / 3))
+        bins = np.array(range(0, Nb)) + 0.5
+        z = np.digitize(np.sqrt(self.K2), bins, right=True)
+        Ek = np.zeros(Nb)
+        ll = np.zeros(Nb)
+        for i, k in enumerate(bins[1:]):
+            k0 = bins[i]
+            ii = np.where((z > k0) & (z <= k))
+            ll[i] = len(ii[0])
+            Ek[i] = (k ** 3 - k0 ** 3) * np.sum(uiui[ii])
+        for i in range(Nb):
+            if ll[i] != 0:
+                Ek[i] = Ek[i] / ll[i]
+        return Ek, bins
+
+    def shell_spectrum(self, uh):
+        """E(k) = 1/2 sum_{k-1/2 < |k| <= k+1/2} |u_hat|^2 (integer shells, full spectrum)."""
+        w = self.hermitian_weights()
+        e = 0.5 * np.sum(np.abs(uh.astype(np.complex128)) ** 2, axis=0) * w
+        kmag = np.sqrt(self.K2) * (self.L[0] / (2 * np.pi))
+        idx = np.floor(kmag + 0.5).astype(np.int64)
+        nb = int(idx.max()) + 1
+        return np.bincount(idx.ravel(), weights=e.ravel(), minlength=nb)
+
+    def cfl_rate(self, uh):
+        """max over points of |u|/dx + |v|/dy + |w|/dz of the dealiased field."""
+        u = self.backward(uh * self.mask)
+        dx = [self.L[i] / self.N[i] for i in range(3)]
+        return float(np.max(np.abs(u[0]) / dx[0] + np.abs(u[1]) / dx[1] + np.abs(u[2]) / dx[2]))
+
+    # --- build-defined forcing ------------------------------------------
+    def forcing_source(self, uh, eps, kf):
+        """Constant-power forcing on 0 < |k| <= kf as a Source term.
+
+        Source = eps / (2 E_f) * u_hat on the shell, with E_f the kinetic
+        energy of the shell (full-spectrum sum).  The injected power
+        Re<Source, u_hat> equals eps at the start of the step.
+        """
+        shell = (self.K2 <= kf * kf + 1e-12) & (self.K2 > 0)
+        w = self.hermitian_weights()
+        Ef = 0.5 * float(np.sum((np.abs(uh.astype(np.complex128)) ** 2) * w * shell))
+        src = np.zeros_like(uh)
+        if Ef > 0:
+            src[:] = (eps / (2.0 * Ef)) * uh * shell
+        return src
+
+
+def taylor_green(grid: Grid):
+    """TG initial velocity (demo/TG.py:23-28) in physical space."""
+    x0 = grid.X[0][:, None, None]
+    x1 = grid.X[1][None, :, None]
+    x2 = grid.X[2][None, None, :]
+    U = np.empty((3,) + grid.N, dtype=grid.dtype)
+    U[0] = np.sin(x0) * np.cos(x1) * np.cos(x2)
+    U[1] = -np.cos(x0) * np.sin(x1) * np.cos(x2)
+    U[2] = 0
+    return U
+
+
+def run_tg(N, steps=10, dt=0.01, nu=0.000625, L=(2 * np.pi,) * 3, dtype=np.float64):
+    """TG run as in demo/TG.py; returns (k, w, u_hat)."""
+    g = Grid(N, L, nu, dtype=dtype)
+    uh = g.forward(taylor_green(g))
+    for _ in range(steps):
+        uh = g.rk4_step(uh, dt)
+    return g.kinetic_energy(uh), g.enstrophy(uh), uh

@@ -1,0 +1,174 @@
+// Line-FFT engine for the pseudo-spectral Navier-Stokes kernels (sm_103a).
+//
+// A "line" is one 1-D transform of length N (a power of two, 16..1024).  A
+// group of G = N/E lanes of one warp owns a line; every lane keeps E = 16 (or
+// 32 for N = 1024) complex values in registers and the line is exchanged
+// between radix passes through a padded shared-memory buffer.  The passes are
+// the Stockham autosort formulation (Govindaraju et al., "High performance
+// discrete Fourier transforms on graphics processors", SC'08): for pass
+// (Ns, R) the butterfly j reads x[j + r N/R], multiplies by W_{Ns R}^{r (j mod
+// Ns)}, does a radix-R DFT in registers and writes x'[(j - j mod Ns) R + j mod
+// Ns + r Ns].  Radices are 16,16,...,N/16^a.  Twiddles come from a table
+// generated in FP64 on the host and rounded to the working precision.
+//
+// Sign convention: S = -1 forward (exp(-2 pi i nk/N)), S = +1 inverse
+// (unnormalised).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sdns {
+
+template <typename R> struct cplx_of;
+template <> struct cplx_of<float> { using type = float2; };
+template <> struct cplx_of<double> { using type = double2; };
+
+template <typename C> __device__ __forceinline__ C mk(decltype(C::x) x, decltype(C::x) y) { C c; c.x = x; c.y = y; return c; }
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return mk<C>(a.x + b.x, a.y + b.y); }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return mk<C>(a.x - b.x, a.y - b.y); }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+  return mk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename C> __device__ __forceinline__ C cconj(C a) { return mk<C>(a.x, -a.y); }
+template <typename C, typename T> __device__ __forceinline__ C cscale(C a, T s) { return mk<C>(a.x * s, a.y * s); }
+// multiply by S*i  (S=-1: -i z, S=+1: i z)
+template <int S, typename C> __device__ __forceinline__ C mul_si(C a) {
+  return S < 0 ? mk<C>(a.y, -a.x) : mk<C>(-a.y, a.x);
+}
+// multiply by the constant (cr + S*ci*i)
+template <int S, typename C> __device__ __forceinline__ C mulc(C a, double cr, double ci) {
+  using T = decltype(C::x);
+  const T r = (T)cr, i = (T)(S * ci);
+  return mk<C>(a.x * r - a.y * i, a.x * i + a.y * r);
+}
+
+// constants cos(pi/8), sin(pi/8), sqrt(1/2)
+#define SDNS_C8 0.92387953251128675613
+#define SDNS_S8 0.38268343236508977173
+#define SDNS_R2 0.70710678118654752440
+
+template <int S, typename C> __device__ __forceinline__ void dft2(C& a, C& b) {
+  C t = a; a = cadd(t, b); b = csub(t, b);
+}
+template <int S, typename C> __device__ __forceinline__ void dft4(C& a, C& b, C& c, C& d) {
+  C t0 = cadd(a, c), t1 = csub(a, c), t2 = cadd(b, d), t3 = mul_si<S>(csub(b, d));
+  a = cadd(t0, t2); c = csub(t0, t2); b = cadd(t1, t3); d = csub(t1, t3);
+}
+template <int S, typename C> __device__ __forceinline__ void dft8(C* v) {
+  C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+  C o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+  dft4<S>(e0, e1, e2, e3);
+  dft4<S>(o0, o1, o2, o3);
+  o1 = mulc<S>(o1, SDNS_R2, SDNS_R2);   // W8^1
+  o2 = mul_si<S>(o2);                   // W8^2
+  o3 = mulc<S>(o3, -SDNS_R2, SDNS_R2);  // W8^3
+  v[0] = cadd(e0, o0); v[4] = csub(e0, o0);
+  v[1] = cadd(e1, o1); v[5] = csub(e1, o1);
+  v[2] = cadd(e2, o2); v[6] = csub(e2, o2);
+  v[3] = cadd(e3, o3); v[7] = csub(e3, o3);
+}
+// W16^m = (cos(pi m/8), S sin(pi m/8))
+template <int S, typename C> __device__ __forceinline__ void dft16(C* v) {
+  // n = 4 n1 + n2 ; k = k1 + 4 k2
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) dft4<S>(v[n2], v[4 + n2], v[8 + n2], v[12 + n2]);
+  // now v[4 k1 + n2] holds y[n2][k1]; twiddle by W16^{n2 k1}
+  v[4 * 1 + 1] = mulc<S>(v[4 * 1 + 1], SDNS_C8, SDNS_S8);    // m=1
+  v[4 * 2 + 1] = mulc<S>(v[4 * 2 + 1], SDNS_R2, SDNS_R2);    // m=2
+  v[4 * 3 + 1] = mulc<S>(v[4 * 3 + 1], SDNS_S8, SDNS_C8);    // m=3
+  v[4 * 1 + 2] = mulc<S>(v[4 * 1 + 2], SDNS_R2, SDNS_R2);    // m=2
+  v[4 * 2 + 2] = mul_si<S>(v[4 * 2 + 2]);                     // m=4
+  v[4 * 3 + 2] = mulc<S>(v[4 * 3 + 2], -SDNS_R2, SDNS_R2);   // m=6
+  v[4 * 1 + 3] = mulc<S>(v[4 * 1 + 3], SDNS_S8, SDNS_C8);    // m=3
+  v[4 * 2 + 3] = mulc<S>(v[4 * 2 + 3], -SDNS_R2, SDNS_R2);   // m=6
+  v[4 * 3 + 3] = mulc<S>(v[4 * 3 + 3], -SDNS_C8, -SDNS_S8);  // m=9
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) dft4<S>(v[4 * k1 + 0], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+  // v[4 k1 + k2] holds X[k1 + 4 k2]; transpose to natural order
+  C t[16];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) t[k1 + 4 * k2] = v[4 * k1 + k2];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = t[i];
+}
+
+template <int R, int S, typename C> __device__ __forceinline__ void dftR(C* v) {
+  if constexpr (R == 2) dft2<S>(v[0], v[1]);
+  else if constexpr (R == 4) dft4<S>(v[0], v[1], v[2], v[3]);
+  else if constexpr (R == 8) dft8<S>(v);
+  else dft16<S>(v);
+}
+
+// padded shared-memory index of line position p (breaks stride-16 bank conflicts)
+__device__ __forceinline__ int padp(int p) { return p + (p >> 4); }
+__host__ __device__ inline int line_ld(int n) {
+  int ld = n + ((n - 1) >> 4);
+  return (ld & 1) ? ld : ld + 1;
+}
+// twiddle table length for an axis of n points: sum over passes of R*Ns
+__host__ __device__ inline int tw_len(int n) {
+  int len = 0, ns = 1;
+  while (ns < n) { int r = (n / ns) >= 16 ? 16 : n / ns; len += r * ns; ns *= r; }
+  return len;
+}
+
+// One Stockham pass of radix R on a line held in `buf` (padded positions).
+template <int R, int E, int S, typename C>
+__device__ __forceinline__ void stockham_pass(C* buf, int g, int G, int N, int Ns, const C* __restrict__ tw) {
+  constexpr int NB = E / R;
+  const int NR = N / R;
+  C v[E];
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const int j = g + G * q;
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[q * R + r] = buf[padp(j + r * NR)];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const int j = g + G * q;
+    const int k = j & (Ns - 1);
+    if (Ns > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        C w = tw[r * Ns + k];
+        if (S > 0) w.y = -w.y;
+        v[q * R + r] = cmul(v[q * R + r], w);
+      }
+    }
+    dftR<R, S>(&v[q * R]);
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const int j = g + G * q;
+    const int k = j & (Ns - 1);
+    const int idx = (j - k) * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) buf[padp(idx + r * Ns)] = v[q * R + r];
+  }
+  __syncwarp();
+}
+
+// Full in-place transform of a line in `buf` (natural order in and out).
+// All 32 lanes of the warp must call this (it uses __syncwarp).
+template <int E, int S, typename C>
+__device__ __forceinline__ void line_fft(C* buf, int g, int N, const C* __restrict__ tw) {
+  const int G = N / E;
+  int Ns = 1, off = 0;
+  while (Ns < N) {
+    const int R = (N / Ns) >= 16 ? 16 : N / Ns;
+    switch (R) {
+      case 16: stockham_pass<16, E, S>(buf, g, G, N, Ns, tw + off); break;
+      case 8: stockham_pass<8, E, S>(buf, g, G, N, Ns, tw + off); break;
+      case 4: stockham_pass<4, E, S>(buf, g, G, N, Ns, tw + off); break;
+      default: stockham_pass<2, E, S>(buf, g, G, N, Ns, tw + off); break;
+    }
+    off += R * Ns;
+    Ns *= R;
+  }
+}
+
+}  // namespace sdns

@@ -1,0 +1,93 @@
+// Internal declarations shared by the kernel translation units and the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sdns {
+
+// Axis description.  A complex axis of n points stores either all n
+// positions (kc < 0) or the 2kc+1 kept wave indices in FFT order
+// [0..kc, -kc..-1] ("compact" rows).  The R2C axis stores kz = 0..Kz-1,
+// padded to Kzp.
+struct RowMap {
+  int n;   // transform length
+  int kc;  // cutoff, < 0 means all positions stored
+  __host__ __device__ int rows() const { return kc < 0 ? n : 2 * kc + 1; }
+  __host__ __device__ int pos(int r) const { return (kc < 0 || r <= kc) ? r : n - (2 * kc + 1) + r; }
+  // signed integer wave index of a stored row
+  __host__ __device__ int wave(int r) const {
+    int p = pos(r);
+    return p < (n + 1) / 2 ? p : p - n;
+  }
+};
+
+// Batched transform along one strided axis.  Line l of field f starts at
+// f*fs + (l / B)*ss + (l % B); position row r adds r*rs.  Lines l are
+// consecutive in memory within runs of B.
+struct AxisArgs {
+  const void* in;
+  void* out;
+  RowMap min, mout;          // input rows, output rows (same n)
+  long long in_fs, in_ss, in_rs;
+  long long out_fs, out_ss, out_rs;
+  long long nlines;          // lines per field
+  long long B;               // contiguous run length of lines
+  int nfield;
+  double scale;              // applied to outputs
+  const void* tw;            // twiddle table of this axis (forward sign)
+  // curl prologue (inverse x sweep): wave-number scales and the compact
+  // geometry of the batch index b = k1row*Kzp + kz
+  double kscale[3];
+  RowMap m1;                 // rows of axis 1 (for k1 of the batch index)
+  int Kzp;
+};
+
+// Fused z-line sweep: C2R of 6 spectral fields, u x w, R2C of 3 fields.
+struct ZArgs {
+  const void* in;            // [nf][nlines][Kzp] complex
+  void* out;                 // [3][nlines][Kzp] complex (may alias in)
+  void* phys;                // [nf][nlines][n] real (C2R-only / R2C-only modes)
+  long long nlines;
+  int n;                     // z transform length
+  int Kz, Kzp;               // stored kz modes and padded pitch
+  int nf;                    // number of fields (modes 1, 2)
+  const void* tw;
+  double inv_dx[3];          // for the CFL rate
+  double* cfl_rate;          // nullptr: no CFL reduction
+};
+
+// Final x sweep with projection, diffusion, source and the RK4 stage update.
+struct RKArgs {
+  const void* in;            // [3][N0][K1][Kzp] complex (after forward y)
+  RowMap m0, m1;             // rows of axis 0 and 1 of the compact layout
+  int Kz, Kzp;
+  long long nlines;          // K1*Kzp
+  double scale;              // 1/(N0 N1 N2)
+  const void* tw;
+  double kscale[3];
+  double nu;
+  int stage;                 // 0..3 RK4 stage, 4 = ComputeRHS only
+  double a, b;               // RK4 coefficients of this stage
+  const double* dt;          // device scalar
+  void* Y;                   // Real complex compact stage input / output
+  double2* S;                // FP64 compact step-start state
+  double2* A;                // FP64 compact accumulator
+  void* rhs_out;             // stage 4: Real complex compact rhs
+  void* p_out;               // optional Real complex compact P_hat
+  const double2* source;     // optional FP64 compact source
+  const double* force_alpha; // optional device scalar; forcing on 0 < K2 <= kf2
+  double kf2;
+  double* partials;          // [gridDim.x][4] energy, enstrophy sums (stage 3)
+};
+
+template <typename Real> struct Kernels {
+  static int axis_plain(const AxisArgs& a, int sign, cudaStream_t s);
+  static int axis_curl_inv(const AxisArgs& a, cudaStream_t s);
+  static int zline_ns(const ZArgs& a, cudaStream_t s);
+  static int zline_c2r(const ZArgs& a, cudaStream_t s);
+  static int zline_r2c(const ZArgs& a, cudaStream_t s);
+  static int axis_rk(const RKArgs& a, cudaStream_t s, int* nblocks_out);
+  static int smem_optin(int dev);
+};
+
+}  // namespace sdns

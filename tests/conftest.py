@@ -1,0 +1,20 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a) and the built libsdns_gb300.so")
+
+
+@pytest.fixture(scope="session")
+def built_lib():
+    """Build (if stale) and load the CUDA library; GPU tests fail loudly without it."""
+    from spectraldns_gb300 import build, _lib
+    build.build()
+    return _lib.lib()
