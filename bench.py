@@ -1,0 +1,358 @@
+#!/usr/bin/env python
+"""Benchmark of the pseudo-spectral Navier-Stokes RK4 step on one GB300.
+
+Workload (the 512^3 case of the headline metric "RK4 steps/s at 512^3 FP32 vs
+FP64"): forced isotropic turbulence on a 512^3 grid in [0, 2pi)^3, seeded
+solenoidal initial field with E(k) ~ k^4 exp(-2 (k/4)^2) and total energy
+0.5, constant-power forcing eps = 0.1 on |k| <= 2, nu = 8e-4, RK4 with CFL
+0.5 (dt from the velocity maximum at every step start), 2/3-rule dealiasing.
+A "step" is one RK4 step (four right-hand-side evaluations).  All inputs are
+synthetic (generated from the seed) and larger than L2 (the state alone is
+1.6 GB), so no L2 flush is needed between steps.
+
+Arms:
+  python bench.py [--gpus N --steps K --warmup W]          this library
+  python bench.py --impl reference [...]                   CPU float32 NumPy/scipy.fft
+      restatement of the reference path (the oracle port) on all host cores
+Under torchrun each rank runs an independent replica on its own GPU
+(replicas only; the whole-job value is the sum of the replicas' steps/s).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RK4 steps/s at 512^3 FP32 vs FP64; closure-LES speedup at spectrum err <=5%"
+WORKLOAD = ("forced isotropic turbulence 512^3 FP32 (seeded k^4 exp(-2(k/4)^2) field, E=0.5, "
+            "eps=0.1 forcing on |k|<=2, nu=8e-4, RK4 CFL 0.5, 2/3 rule)")
+NU, EPS, KF, CFL, K0 = 0.0008, 0.1, 2.0, 0.5, 4.0
+KERNEL_NAMES = ["x_inv_curl", "y_inv", "z_c2r_cross_r2c", "y_fwd", "x_fwd_project_rk4"]
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    p.add_argument("--n", type=int, default=512)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--les", action="store_true", help="also time the closure LES (if built)")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.path = os.path.join("/tmp", "sdns_clocks_%d_%d.csv" % (os.getpid(), gpu_index))
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(gpu_index)], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes per launch of each kernel class (FP32 state, FP64 RK4 accumulators)
+# ---------------------------------------------------------------------------
+def kernel_bytes(n, csz=8, acc=16):
+    from spectraldns_gb300.init import dealias_cutoff
+    kc = dealias_cutoff(n)
+    K = 2 * kc + 1
+    Kz = kc + 1
+    Kzp = (Kz + 7) // 8 * 8
+    comp = K * K * Kzp          # one compact component
+    a1 = n * K * Kzp            # one field after the first inverse axis
+    a2 = n * n * Kzp            # one field after the second inverse axis
+    rk_state = comp * 3 * ((acc + csz + acc) + 2 * (csz + 3 * acc + csz) + (csz + 2 * acc + csz)) / 4.0
+    return {
+        "x_inv_curl": 3 * comp * csz + 6 * a1 * csz,
+        "y_inv": 6 * a1 * csz + 6 * a2 * csz,
+        "z_c2r_cross_r2c": 6 * n * n * Kz * csz + 3 * a2 * csz,
+        "y_fwd": 3 * a2 * csz + 3 * a1 * csz,
+        "x_fwd_project_rk4": 3 * a1 * csz + rk_state,
+    }
+
+
+def run_ours(args):
+    import torch
+    from spectraldns_gb300.gpu import Context
+    from spectraldns_gb300.init import isotropic_field
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+        torch.cuda.set_device(local)
+    dev = local
+    n = args.n
+    N = (n, n, n)
+    uh0 = isotropic_field(N, k0=K0, energy=0.5, seed=0, dtype=np.complex64)
+    ctx = Context(N, nu=NU, precision="single", device=dev)
+    ctx.set_forcing(EPS, KF)
+    ctx.set_cfl(CFL)
+    ctx.set_state(uh0)
+    for _ in range(args.warmup):
+        ctx.rk4(0.0, 1)
+    ctx.synchronize()
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=torch.device("cuda", dev))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    ctx.set_timing(True)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    clk = Clocks(dev)
+    e0.record(stream)
+    ctx.rk4(0.0, args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    clocks = clk.stop()
+    if ws > 1:
+        torch.distributed.barrier()
+    ms = e0.elapsed_time(e1)
+    ktimes, klaunch = ctx.get_timing()
+    ctx.set_timing(False)
+    diag = ctx.diagnostics()
+    t_ms = torch.tensor([ms], device="cuda:%d" % dev)
+    if ws > 1:
+        torch.distributed.all_reduce(t_ms, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t_ms.item())
+    value = ws * args.steps / (ms_max / 1e3)
+
+    # per-kernel roofline
+    kb = kernel_bytes(n)
+    peak, peak_src = peaks()
+    kernels = {}
+    for i, name in enumerate(KERNEL_NAMES):
+        if klaunch[i] == 0:
+            continue
+        per = ktimes[i] / klaunch[i]
+        kernels[name] = {"ms_per_launch": per, "launches": klaunch[i], "share": ktimes[i] / max(sum(ktimes), 1e-30),
+                         "alg_bytes": kb[name], "gbs": kb[name] / (per * 1e-3) / 1e9}
+    dom = max(kernels, key=lambda k: kernels[k]["ms_per_launch"] * kernels[k]["launches"])
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
+            tr = json.load(f)
+        if str(n) in tr and dom in tr[str(n)]:
+            traffic = tr[str(n)][dom]
+    except Exception:
+        pass
+    step_bytes = sum(kernels[k]["alg_bytes"] * kernels[k]["launches"] for k in kernels) / args.steps
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": kernels[dom]["gbs"], "peak": peak, "unit": "GB/s",
+                "frac": kernels[dom]["gbs"] / peak, "traffic": traffic, "peak_source": peak_src,
+                "step_alg_bytes": step_bytes,
+                "step_achieved_gbs": step_bytes / (ms / args.steps * 1e-3) / 1e9}
+    roofline["step_frac"] = roofline["step_achieved_gbs"] / peak
+    launches = sum(klaunch) + args.steps * 3  # + step-begin, CFL dt and step-end kernels
+
+    out = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded spectrum, generated on the host; no dataset)",
+           "config": {"workload": WORKLOAD, "grid": [n, n, n], "precision": "single (FP32 transforms, FP64 RK4 "
+                      "accumulators and reductions)", "l2": "inputs larger than L2 (1.6 GB state), no flush",
+                      "parallelism": "replicas" if ws > 1 else "single GPU",
+                      "timing": "CUDA events on the solver stream; per-kernel events in the same region"},
+           "roofline": roofline, "kernels": kernels, "gpu_launches": launches, "clocks": clocks,
+           "final_energy": diag["energy"], "final_time": diag["time"]}
+
+    # end to end through the public API with pinned host buffers
+    if not args.no_e2e:
+        ke = max(3, min(args.steps, 10))
+        shape = ctx.spec_shape
+        hin = torch.empty(shape, dtype=torch.complex64, pin_memory=True)
+        hout = torch.empty(shape, dtype=torch.complex64, pin_memory=True)
+        hin.numpy()[...] = uh0
+        ctx.set_state(hin)
+        ctx.rk4(0.0, 1)
+        ctx.get_state(hout)
+        if ws > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            ctx.set_state(hin)       # host -> device: this step's input state
+            ctx.rk4(0.0, 1)
+            ctx.get_state(hout)      # device -> host: the step's result (synchronous)
+        te = time.perf_counter() - t0
+        tt = torch.tensor([te], device="cuda:%d" % dev)
+        if ws > 1:
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        nbytes = int(np.prod(shape)) * 8
+        out["e2e"] = {"value": ws * ke / float(tt.item()), "unit": "steps/s", "h2d_bytes_per_step": nbytes,
+                      "d2h_bytes_per_step": nbytes, "steps": ke,
+                      "path": "Context.set_state(pinned host) + rk4 + get_state(pinned host) per step"}
+    ctx.close()
+    del ctx
+
+    if not args.no_fp64:
+        c64 = Context(N, nu=NU, precision="double", device=dev)
+        c64.set_forcing(EPS, KF)
+        c64.set_cfl(CFL)
+        c64.set_state(uh0.astype(np.complex128))
+        c64.rk4(0.0, 2)
+        c64.synchronize()
+        st = torch.cuda.ExternalStream(c64.stream_handle(), device=torch.device("cuda", dev))
+        k64 = max(3, args.steps // 10)
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(st)
+        c64.rk4(0.0, k64)
+        a1.record(st)
+        torch.cuda.synchronize(dev)
+        m64 = a0.elapsed_time(a1)
+        out["fp64"] = {"value": ws * k64 / (m64 / 1e3), "unit": "steps/s", "steps": k64,
+                       "ms_per_step": m64 / k64, "dtype": "f64"}
+        c64.close()
+
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_sample(512 if n >= 512 else n)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_stage(n, workers):
+    """One RK4 stage (ComputeRHS + stage update) of the float32 oracle port at n^3."""
+    from oracle.ns_ref import Grid
+    from spectraldns_gb300.init import isotropic_field
+    g = Grid((n, n, n), nu=NU, dtype=np.float32, workers=workers)
+    uh = isotropic_field((n, n, n), k0=K0, seed=0, dtype=np.complex64)
+    u1 = uh.copy()
+
+    def stage():
+        rhs = g.compute_rhs(uh)
+        u0 = u1 + np.float32(0.5 * 1e-3) * rhs
+        u1[...] += np.float32(1e-3 / 6) * rhs
+        return u0
+    return stage
+
+
+def cpu_sample(n):
+    workers = os.cpu_count() or 1
+    stage = cpu_stage(n, workers)
+    t0 = time.perf_counter()
+    stage()
+    t = time.perf_counter() - t0
+    return {"value": 1.0 / (4 * t), "unit": "steps/s", "cores": workers, "kind": "port",
+            "sample": "one RK4 stage (ComputeRHS + stage update) of the float32 NumPy/scipy.fft oracle at %d^3 on "
+                      "%d threads, %.1f s; steps/s = 1/(4 x stage time)" % (n, workers, t)}
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    workers = os.cpu_count() or 1
+    n = args.n
+    nsteps = args.steps + args.warmup
+    # a bounded per-step sample: one RK4 stage, on a grid small enough for the whole run to fit in a few minutes
+    ns = n
+    for cand in (n, n // 2, n // 4, n // 8):
+        ns = cand
+        est = 12.0 * (cand / 512.0) ** 3 * (math.log2(cand ** 3) / 27.0) if cand > 0 else 0
+        if est * nsteps <= 200.0:
+            break
+    stage = cpu_stage(ns, workers)
+    for _ in range(args.warmup):
+        stage()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        stage()
+    t = (time.perf_counter() - t0) / args.steps
+    scale = (n / ns) ** 3 * (math.log2(n ** 3) / math.log2(ns ** 3))
+    value = 1.0 / (4 * t * scale)
+    sample = ("each step: one RK4 stage (ComputeRHS + stage update) of the float32 NumPy/scipy.fft restatement of "
+              "spectralDNS NS.py at %d^3 on %d threads (%.3f s)" % (ns, workers, t))
+    if ns != n:
+        sample += "; scaled to %d^3 by the N^3 log N work ratio %.2f" % (n, scale)
+    out = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 4 * t * scale * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded spectrum)", "impl": "reference",
+           "config": {"workload": WORKLOAD, "grid": [n, n, n], "parallelism": "host threads"},
+           "cpu_baseline": {"value": value, "unit": "steps/s", "cores": workers, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

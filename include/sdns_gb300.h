@@ -87,6 +87,9 @@ const char* sdns_last_error(void);
 int sdns_create(const sdns_config* cfg, sdns_ctx** out);
 int sdns_destroy(sdns_ctx* ctx);
 int sdns_synchronize(sdns_ctx* ctx);
+/* the context's CUDA stream (cudaStream_t), for callers that time or order
+ * their own work against the solver's kernels */
+int sdns_get_stream(sdns_ctx* ctx, void** stream);
 /* bytes of device memory held by the context */
 int sdns_memory_bytes(sdns_ctx* ctx, int64_t* bytes);
 

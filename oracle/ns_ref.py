@@ -97,11 +97,13 @@ class Grid:
         # Nyquist index of the complex axes is -n/2 (fftfreq); the R2C
         # Nyquist +n2/2 is outside every kept set.
         scale = [2 * np.pi / l for l in self.L]
-        k1d = [self.ki[i].astype(np.float64) * scale[i] for i in range(3)]
+        # K cast to the working float type as NS.py:39-41 does
+        k1d = [(self.ki[i].astype(np.float64) * scale[i]).astype(self.dtype) for i in range(3)]
         self.K = [k1d[0][:, None, None], k1d[1][None, :, None], k1d[2][None, None, :]]
         self.K2 = self.K[0] ** 2 + self.K[1] ** 2 + self.K[2] ** 2
-        K2n = np.where(self.K2 == 0, 1.0, self.K2)
+        K2n = np.where(self.K2 == 0, self.dtype.type(1), self.K2)
         self.K_over_K2 = [self.K[i] / K2n for i in range(3)]
+        self.nu = self.dtype.type(self.nu)
         self.kc = [dealias_cutoff(n, dealias) for n in self.N]
         m0 = np.abs(self.ki[0]) <= self.kc[0]
         m1 = np.abs(self.ki[1]) <= self.kc[1]
@@ -136,7 +138,7 @@ class Grid:
     @staticmethod
     def cross(a, b):
         """cross1: a x b for real fields (maths/cross.py:13-25)."""
-        c = np.empty_like(a)
+        c = np.empty(a.shape, dtype=np.result_type(a, b))
         c[0] = a[1] * b[2] - a[2] * b[1]
         c[1] = a[2] * b[0] - a[0] * b[2]
         c[2] = a[0] * b[1] - a[1] * b[0]
@@ -151,8 +153,9 @@ class Grid:
         nl = self.forward(self.cross(u, w)) * m
         P = nl[0] * self.K_over_K2[0] + nl[1] * self.K_over_K2[1] + nl[2] * self.K_over_K2[2]
         rhs = np.empty_like(uh)
+        nuK2 = self.nu * self.K2
         for i in range(3):
-            rhs[i] = nl[i] - P * self.K[i] - self.nu * self.K2 * uh[i]
+            rhs[i] = nl[i] - P * self.K[i] - nuK2 * uh[i]
         if source is not None:
             rhs += source
         if return_parts:

@@ -46,6 +46,7 @@ SIGNATURES = {
     "sdns_create": (C.c_int, [C.POINTER(sdns_config), C.POINTER(_CTX)]),
     "sdns_destroy": (C.c_int, [_CTX]),
     "sdns_synchronize": (C.c_int, [_CTX]),
+    "sdns_get_stream": (C.c_int, [_CTX, C.POINTER(C.c_void_p)]),
     "sdns_memory_bytes": (C.c_int, [_CTX, C.POINTER(C.c_int64)]),
     "sdns_set_state": (C.c_int, [_CTX, _P, C.c_int]),
     "sdns_get_state": (C.c_int, [_CTX, _P, C.c_int]),

@@ -838,6 +838,12 @@ int sdns_synchronize(sdns_ctx* c) {
   return SDNS_OK;
 }
 
+int sdns_get_stream(sdns_ctx* c, void** stream) {
+  if (!c || !stream) return fail(SDNS_EINVAL, "null argument");
+  *stream = (void*)c->st;
+  return SDNS_OK;
+}
+
 int sdns_memory_bytes(sdns_ctx* c, int64_t* bytes) {
   if (!c || !bytes) return fail(SDNS_EINVAL, "null argument");
   *bytes = c->bytes;

@@ -168,6 +168,12 @@ class Context:
     def synchronize(self):
         check(self._L.sdns_synchronize(self._h))
 
+    def stream_handle(self):
+        """Raw cudaStream_t of the context (wrap with torch.cuda.ExternalStream)."""
+        s = C.c_void_p()
+        check(self._L.sdns_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
     def _transform(self, fn, a, out, in_dtype, out_dtype, in_tail, out_tail):
         shp = tuple(np.shape(a)) if not _is_torch(a) else tuple(a.shape)
         nf = 1 if len(shp) == 3 else shp[0]
