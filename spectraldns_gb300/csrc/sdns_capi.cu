@@ -81,13 +81,13 @@ struct sdns_ctx {
   double kscale[3];
   // device buffers
   void* Y = nullptr;         // Real complex compact
-  double2* S = nullptr;      // FP64 compact
-  double2* A = nullptr;      // FP64 compact
+  void* S = nullptr;         // compact step-start state, Acc<Real>::T (16 B per mode)
+  void* A = nullptr;         // compact RK4 accumulator, Acc<Real>::T
   void* T1 = nullptr;        // [6][N0][K1][Kzp]
   void* T2 = nullptr;        // [6][N0][N1][Kzp]
   void* Pc = nullptr;        // compact P_hat
   void* Yx = nullptr;        // compact input of compute_rhs
-  double2* src = nullptr;    // compact source
+  void* src = nullptr;       // compact source, Acc<Real>::T
   void* src_full = nullptr;  // caller-layout source (compute_rhs outside modes)
   void* H = nullptr;         // caller-layout modes outside the dealiased set
   bool high = false;
@@ -146,7 +146,9 @@ struct Geo {
 
 // caller layout [3][N0][N1][N2h] -> compact Y (Real) and S (FP64)
 template <typename C>
-__global__ void k_gather(const C* full, C* Y, double2* S, Geo g, long long ncomp1) {
+__global__ void k_gather(const C* full, C* Y, void* Sv, Geo g, long long ncomp1) {
+  using AC = Acc<decltype(C::x)>;
+  typename AC::T* S = reinterpret_cast<typename AC::T*>(Sv);
   const long long n = 3 * ncomp1;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const long long c = i / ncomp1;
@@ -162,7 +164,7 @@ __global__ void k_gather(const C* full, C* Y, double2* S, Geo g, long long ncomp
       v = full[fi];
     }
     if (Y) Y[i] = v;
-    if (S) S[i] = make_double2((double)v.x, (double)v.y);
+    if (S) AC::put(S, i, (double)v.x, (double)v.y);
   }
 }
 
@@ -185,9 +187,11 @@ __global__ void k_outside(const C* full, Geo g, int* flag) {
 // compact (FP64 or Real) -> full layout with pitch `pitch` (N2h for the caller
 // layout, Kzpf for the padded transform layout).  Outside modes: from
 // `outside` (same layout as the caller array) or zero.  mult = 0: x1, 1: x(-i)
-template <typename C, typename SRC>
-__global__ void k_scatter(const SRC* comp, C* full, const C* outside, Geo g, int nf, int pitch, long long ncomp1,
-                          int mult) {
+// comp_is_acc: the compact source is the accumulator format (S), else Real complex
+template <typename C>
+__global__ void k_scatter(const void* comp, int comp_is_acc, C* full, const C* outside, Geo g, int nf, int pitch,
+                          long long ncomp1, int mult) {
+  using AC = Acc<decltype(C::x)>;
   const long long n1 = (long long)g.N0 * g.N1 * pitch, n = nf * n1;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const long long c = i / n1;
@@ -200,9 +204,13 @@ __global__ void k_scatter(const SRC* comp, C* full, const C* outside, Geo g, int
     if (kz < g.N2h) {
       if (g.inside(p0, p1, kz)) {
         const long long ci = c * ncomp1 + ((long long)g.row(g.m0, p0) * g.m1.rows() + g.row(g.m1, p1)) * g.Kzp + kz;
-        const SRC s = comp[ci];
-        v.x = (decltype(v.x))s.x;
-        v.y = (decltype(v.x))s.y;
+        if (comp_is_acc) {
+          const double2 s = AC::get(reinterpret_cast<const typename AC::T*>(comp), ci);
+          v.x = (decltype(v.x))s.x;
+          v.y = (decltype(v.x))s.y;
+        } else {
+          v = reinterpret_cast<const C*>(comp)[ci];
+        }
       } else if (outside) {
         v = outside[((c * g.N0 + p0) * g.N1 + p1) * g.N2h + kz];
       }
@@ -295,8 +303,10 @@ __global__ void k_curl_div(const C* u, C* out, Geo g, int div) {
 }
 
 // start of an RK4 step: reset the CFL maximum, forcing coefficient from S
-__global__ void k_step_begin(const double2* S, Geo g, long long ncomp1, double* sc, double eps, double kf2, int kfi0,
+template <typename Real>
+__global__ void k_step_begin(const void* Sv, Geo g, long long ncomp1, double* sc, double eps, double kf2, int kfi0,
                              int kfi1, int kfi2) {
+  const typename Acc<Real>::T* S = reinterpret_cast<const typename Acc<Real>::T*>(Sv);
   __shared__ double red[32];
   double e = 0.0;
   if (eps > 0.0) {
@@ -310,7 +320,10 @@ __global__ void k_step_begin(const double2* S, Geo g, long long ncomp1, double* 
       const int r0 = j0 >= 0 ? j0 : j0 + 2 * g.m0.kc + 1, r1 = j1 >= 0 ? j1 : j1 + 2 * g.m1.kc + 1;
       const long long o = ((long long)r0 * g.m1.rows() + r1) * g.Kzp + kz;
       const double w = kz == 0 ? 0.5 : 1.0;
-      for (int c = 0; c < 3; ++c) { const double2 v = S[c * ncomp1 + o]; e += w * (v.x * v.x + v.y * v.y); }
+      for (int c = 0; c < 3; ++c) {
+        const double2 v = Acc<Real>::get(S, c * ncomp1 + o);
+        e += w * (v.x * v.x + v.y * v.y);
+      }
     }
   }
   for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
@@ -351,7 +364,9 @@ __global__ void k_step_end(const double* partials, long long nb, double* sc) {
 // float64 sums over the compact state (+ outside modes in H): 1/2 sum |u|^2,
 // 1/2 sum |K x u|^2, 1/2 sum |K.u|^2
 template <typename C>
-__global__ void k_diag(const double2* S, const C* H, Geo g, long long ncomp1, double* part) {
+__global__ void k_diag(const void* Sv, const C* H, Geo g, long long ncomp1, double* part) {
+  using AC = Acc<decltype(C::x)>;
+  const typename AC::T* S = reinterpret_cast<const typename AC::T*>(Sv);
   __shared__ double red[3][32];
   double s[3] = {0, 0, 0};
   const long long n1 = (long long)g.m0.rows() * g.m1.rows() * g.Kzp;
@@ -360,7 +375,7 @@ __global__ void k_diag(const double2* S, const C* H, Geo g, long long ncomp1, do
     if (kz >= g.Kz) continue;
     const int r1 = (int)((i / g.Kzp) % g.m1.rows()), r0 = (int)(i / ((long long)g.Kzp * g.m1.rows()));
     const double k0 = g.ks[0] * g.m0.wave(r0), k1 = g.ks[1] * g.m1.wave(r1), k2 = g.ks[2] * kz;
-    const double2 a = S[i], b = S[ncomp1 + i], c = S[2 * ncomp1 + i];
+    const double2 a = AC::get(S, i), b = AC::get(S, ncomp1 + i), c = AC::get(S, 2 * ncomp1 + i);
     const double w = (kz == 0 || 2 * kz == 2 * (g.N2h - 1)) ? 0.5 : 1.0;
     s[0] += w * (a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y + c.x * c.x + c.y * c.y);
     const double xr = k1 * c.x - k2 * b.x, xi = k1 * c.y - k2 * b.y;
@@ -405,8 +420,10 @@ __global__ void k_diag(const double2* S, const C* H, Geo g, long long ncomp1, do
 
 // shell spectrum of demo/Isotropic.py:88-114: bin i collects i+0.5 < |K| <= i+1.5
 template <typename C>
-__global__ void k_spectrum(const double2* S, const C* H, Geo g, long long ncomp1, double* sums, double* counts,
+__global__ void k_spectrum(const void* Sv, const C* H, Geo g, long long ncomp1, double* sums, double* counts,
                            int nb) {
+  using AC = Acc<decltype(C::x)>;
+  const typename AC::T* S = reinterpret_cast<const typename AC::T*>(Sv);
   const long long n1 = (long long)g.m0.rows() * g.m1.rows() * g.Kzp;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n1; i += (long long)gridDim.x * blockDim.x) {
     const int kz = (int)(i % g.Kzp);
@@ -416,7 +433,7 @@ __global__ void k_spectrum(const double2* S, const C* H, Geo g, long long ncomp1
     const double km = sqrt(k0 * k0 + k1 * k1 + k2 * k2);
     const int b = (int)ceil(km - 0.5) - 1;
     if (b < 0 || b > nb - 2) continue;
-    const double2 a = S[i], bb = S[ncomp1 + i], c = S[2 * ncomp1 + i];
+    const double2 a = AC::get(S, i), bb = AC::get(S, ncomp1 + i), c = AC::get(S, 2 * ncomp1 + i);
     const double w = (kz == 0) ? 1.0 : 2.0;
     atomicAdd(&sums[b], w * (a.x * a.x + a.y * a.y + bb.x * bb.x + bb.y * bb.y + c.x * c.x + c.y * c.y));
   }
@@ -571,11 +588,11 @@ int repitch(sdns_ctx* c, const void* in, void* out, int nf, int pin, int pout, i
 int state_to_padded(sdns_ctx* c, void* F) {
   Geo g = geo(c);
   if (c->dbl)
-    k_scatter<double2, double2><<<nblocks(3 * c->npadf1), 256, 0, c->st>>>(
-        c->S, (double2*)F, c->high ? (const double2*)c->H : nullptr, g, 3, c->Kzpf, c->ncomp1, 0);
+    k_scatter<double2><<<nblocks(3 * c->npadf1), 256, 0, c->st>>>(
+        c->S, 1, (double2*)F, c->high ? (const double2*)c->H : nullptr, g, 3, c->Kzpf, c->ncomp1, 0);
   else
-    k_scatter<float2, double2><<<nblocks(3 * c->npadf1), 256, 0, c->st>>>(
-        c->S, (float2*)F, c->high ? (const float2*)c->H : nullptr, g, 3, c->Kzpf, c->ncomp1, 0);
+    k_scatter<float2><<<nblocks(3 * c->npadf1), 256, 0, c->st>>>(
+        c->S, 1, (float2*)F, c->high ? (const float2*)c->H : nullptr, g, 3, c->Kzpf, c->ncomp1, 0);
   CK(cudaGetLastError());
   return SDNS_OK;
 }
@@ -672,7 +689,10 @@ int launch_step(sdns_ctx* c) {
   const double L0 = c->cfg.L[0], L1 = c->cfg.L[1], L2 = c->cfg.L[2];
   const int kfi0 = (int)floor(c->kf * L0 / (2 * M_PI)) + 1, kfi1 = (int)floor(c->kf * L1 / (2 * M_PI)) + 1,
             kfi2 = (int)floor(c->kf * L2 / (2 * M_PI)) + 1;
-  k_step_begin<<<1, 256, 0, c->st>>>(c->S, g, c->ncomp1, c->sc, c->eps, c->kf * c->kf, kfi0, kfi1, kfi2);
+  if (c->dbl)
+    k_step_begin<double><<<1, 256, 0, c->st>>>(c->S, g, c->ncomp1, c->sc, c->eps, c->kf * c->kf, kfi0, kfi1, kfi2);
+  else
+    k_step_begin<float><<<1, 256, 0, c->st>>>(c->S, g, c->ncomp1, c->sc, c->eps, c->kf * c->kf, kfi0, kfi1, kfi2);
   CK(cudaGetLastError());
   for (int rk = 0; rk < 4; ++rk) {
     int e = launch_stage_sweeps(c, c->Y, rk, rk == 0 && c->cfl > 0, nullptr,
@@ -886,11 +906,11 @@ int sdns_get_state(sdns_ctx* c, void* u_hat, int where) {
   if ((e = ensure_stage(c))) return e;
   Geo g = geo(c);
   if (c->dbl)
-    k_scatter<double2, double2><<<nblocks(3 * c->nfull1), 256, 0, c->st>>>(
-        c->S, (double2*)c->stage, c->high ? (const double2*)c->H : nullptr, g, 3, c->N2h, c->ncomp1, 0);
+    k_scatter<double2><<<nblocks(3 * c->nfull1), 256, 0, c->st>>>(
+        c->S, 1, (double2*)c->stage, c->high ? (const double2*)c->H : nullptr, g, 3, c->N2h, c->ncomp1, 0);
   else
-    k_scatter<float2, double2><<<nblocks(3 * c->nfull1), 256, 0, c->st>>>(
-        c->S, (float2*)c->stage, c->high ? (const float2*)c->H : nullptr, g, 3, c->N2h, c->ncomp1, 0);
+    k_scatter<float2><<<nblocks(3 * c->nfull1), 256, 0, c->st>>>(
+        c->S, 1, (float2*)c->stage, c->high ? (const float2*)c->H : nullptr, g, 3, c->N2h, c->ncomp1, 0);
   CK(cudaGetLastError());
   return copy_out(c, u_hat, c->stage, 3 * c->nfull1 * (long long)c->csz, where);
 }
@@ -938,13 +958,13 @@ int sdns_compute_rhs(sdns_ctx* c, const void* u_hat, void* rhs, int where) {
   if ((e = ensure_full_bufs(c))) return e;
   void* out = c->F1;
   if (c->dbl) {
-    k_scatter<double2, double2><<<nblocks(3 * c->nfull1), 256, 0, c->st>>>(
-        (const double2*)c->T2, (double2*)out, nullptr, g, 3, c->N2h, c->ncomp1, 0);
+    k_scatter<double2><<<nblocks(3 * c->nfull1), 256, 0, c->st>>>(
+        c->T2, 0, (double2*)out, nullptr, g, 3, c->N2h, c->ncomp1, 0);
     k_rhs_outside<double2><<<nblocks(3 * c->nfull1), 256, 0, c->st>>>(
         (const double2*)c->stage, (const double2*)c->src_full, (double2*)out, g, c->cfg.nu);
   } else {
-    k_scatter<float2, float2><<<nblocks(3 * c->nfull1), 256, 0, c->st>>>(
-        (const float2*)c->T2, (float2*)out, nullptr, g, 3, c->N2h, c->ncomp1, 0);
+    k_scatter<float2><<<nblocks(3 * c->nfull1), 256, 0, c->st>>>(
+        c->T2, 0, (float2*)out, nullptr, g, 3, c->N2h, c->ncomp1, 0);
     k_rhs_outside<float2><<<nblocks(3 * c->nfull1), 256, 0, c->st>>>(
         (const float2*)c->stage, (const float2*)c->src_full, (float2*)out, g, c->cfg.nu);
   }
@@ -1092,11 +1112,11 @@ int sdns_pressure(sdns_ctx* c, void* p, int where) {
   if ((e = ensure_full_bufs(c))) return e;
   Geo g = geo(c);
   if (c->dbl)
-    k_scatter<double2, double2><<<nblocks(c->npadf1), 256, 0, c->st>>>((const double2*)c->Pc, (double2*)c->F1, nullptr,
-                                                                        g, 1, c->Kzpf, c->ncomp1, 1);
+    k_scatter<double2><<<nblocks(c->npadf1), 256, 0, c->st>>>(c->Pc, 0, (double2*)c->F1, nullptr, g, 1, c->Kzpf,
+                                                               c->ncomp1, 1);
   else
-    k_scatter<float2, float2><<<nblocks(c->npadf1), 256, 0, c->st>>>((const float2*)c->Pc, (float2*)c->F1, nullptr, g,
-                                                                      1, c->Kzpf, c->ncomp1, 1);
+    k_scatter<float2><<<nblocks(c->npadf1), 256, 0, c->st>>>(c->Pc, 0, (float2*)c->F1, nullptr, g, 1, c->Kzpf,
+                                                              c->ncomp1, 1);
   CK(cudaGetLastError());
   if ((e = full_backward(c, c->F1, c->F2, 1))) return e;
   return copy_out(c, p, c->PH, c->nphys1 * (long long)c->rsz, where);

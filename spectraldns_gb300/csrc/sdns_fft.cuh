@@ -171,4 +171,66 @@ __device__ __forceinline__ void line_fft(C* buf, int g, int N, const C* __restri
   }
 }
 
+// First pass (Ns = 1, radix 16) reading its inputs through a loader
+// functor ld(position) instead of from `buf`; the result is written to `buf`
+// in natural order.  The loader may read memory that overlaps `buf`: every
+// lane loads before any lane stores.
+template <int E, int S, typename C, typename Loader>
+__device__ __forceinline__ void stockham_first16(C* buf, int g, int G, int N, Loader& ld) {
+  constexpr int R = 16, NB = E / R;
+  const int NR = N / R;
+  C v[E];
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const int j = g + G * q;
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[q * R + r] = ld(j + r * NR);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < NB; ++q) dftR<R, S>(&v[q * R]);
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const int j = g + G * q;
+#pragma unroll
+    for (int r = 0; r < R; ++r) buf[padp(j * R + r)] = v[q * R + r];
+  }
+  __syncwarp();
+}
+
+template <int E, int S, typename C, typename Loader>
+__device__ __forceinline__ void line_fft_ld(C* buf, int g, int N, const C* __restrict__ tw, Loader& ld) {
+  const int G = N / E;
+  stockham_first16<E, S>(buf, g, G, N, ld);
+  int Ns = 16, off = 16;
+  while (Ns < N) {
+    const int R = (N / Ns) >= 16 ? 16 : N / Ns;
+    switch (R) {
+      case 16: stockham_pass<16, E, S>(buf, g, G, N, Ns, tw + off); break;
+      case 8: stockham_pass<8, E, S>(buf, g, G, N, Ns, tw + off); break;
+      case 4: stockham_pass<4, E, S>(buf, g, G, N, Ns, tw + off); break;
+      default: stockham_pass<2, E, S>(buf, g, G, N, Ns, tw + off); break;
+    }
+    off += R * Ns;
+    Ns *= R;
+  }
+}
+
+// Ampere-style asynchronous global->shared copies (LDGSTS); the data does not
+// pass through registers, so a whole tile can be in flight per thread block.
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+template <int BYTES> __device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+  if constexpr (BYTES == 16) cp_async16(smem, gmem);
+  else cp_async8(smem, gmem);
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 }  // namespace sdns

@@ -5,6 +5,30 @@
 
 namespace sdns {
 
+// ---------------------------------------------------------------------------
+// accumulator storage of the RK4 step-start state S and the accumulator A:
+// FP64 complex (double solver) or compensated FP32 "float-float" complex
+// {re_hi, im_hi, re_lo, im_lo} (single solver).  Both are 16 bytes.
+// ---------------------------------------------------------------------------
+template <typename Real> struct Acc;
+template <> struct Acc<float> {
+  using T = float4;
+  __device__ static double2 get(const T* p, long long i) {
+    const float4 v = p[i];
+    return make_double2((double)v.x + (double)v.z, (double)v.y + (double)v.w);
+  }
+  __device__ static void put(T* p, long long i, double x, double y) {
+    const float hx = (float)x, hy = (float)y;
+    p[i] = make_float4(hx, hy, (float)(x - (double)hx), (float)(y - (double)hy));
+  }
+};
+template <> struct Acc<double> {
+  using T = double2;
+  __device__ static double2 get(const T* p, long long i) { return p[i]; }
+  __device__ static void put(T* p, long long i, double x, double y) { p[i] = make_double2(x, y); }
+};
+
+
 // Axis description.  A complex axis of n points stores either all n
 // positions (kc < 0) or the 2kc+1 kept wave indices in FFT order
 // [0..kc, -kc..-1] ("compact" rows).  The R2C axis stores kz = 0..Kz-1,
@@ -70,11 +94,11 @@ struct RKArgs {
   double a, b;               // RK4 coefficients of this stage
   const double* dt;          // device scalar
   void* Y;                   // Real complex compact stage input / output
-  double2* S;                // FP64 compact step-start state
-  double2* A;                // FP64 compact accumulator
+  void* S;                   // compact step-start state (Acc<Real>::T)
+  void* A;                   // compact accumulator (Acc<Real>::T)
   void* rhs_out;             // stage 4: Real complex compact rhs
   void* p_out;               // optional Real complex compact P_hat
-  const double2* source;     // optional FP64 compact source
+  const void* source;        // optional compact source (Acc<Real>::T)
   const double* force_alpha; // optional device scalar; forcing on 0 < K2 <= kf2
   double kf2;
   double* partials;          // [gridDim.x][4] energy, enstrophy sums (stage 3)

@@ -9,9 +9,10 @@
 //   z: C2R(6) -> u x w -> R2C(3)      -> [3][N0][N1][Kzp]   (in place)
 //   y             [3][N0][N1][Kzp]   -> [3][N0][K1][Kzp]
 //   x + projection + diffusion + source + RK4 update -> compact state
-// The pruned inverse transforms read only the kept rows and zero the rest in
-// shared memory; the pruned forward transforms store only the kept rows
-// (which is the 2/3-rule mask of the nonlinear term).
+// The pruned inverse transforms read only the kept rows (the rest of the line
+// is zero); the pruned forward transforms store only the kept rows (which is
+// the 2/3-rule mask of the nonlinear term).  Tiles are staged into shared
+// memory with cp.async so that a whole tile is in flight per thread block.
 #pragma once
 #include "sdns_fft.cuh"
 #include "sdns_internal.h"
@@ -20,22 +21,38 @@ namespace sdns {
 
 template <typename C> __device__ __forceinline__ C czero() { return mk<C>(0, 0); }
 
+// error-free float-float addition (Knuth TwoSum + renormalisation)
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float x) {
+  const float s = __fadd_rn(hi, x);
+  const float bb = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+  const float t = __fadd_rn(e, lo);
+  hi = __fadd_rn(s, t);
+  lo = __fsub_rn(t, __fsub_rn(hi, s));
+}
+
 // ---------------------------------------------------------------------------
-// strided axis sweep: MODE 0 plain copy prologue, MODE 1 curl prologue
+// strided axis sweep.  MODE 0: out field f = transform of in field f.
+// MODE 1 (inverse x with curl): out fields 0-2 = u_hat, 3-5 = i K x u_hat;
+// the two components of a curl field are staged and combined in the first
+// radix pass.
 // ---------------------------------------------------------------------------
 template <typename Real, int E, int S, int MODE>
-__global__ void __launch_bounds__(256) k_axis(AxisArgs a) {
+__global__ void __launch_bounds__(256, 3) k_axis(AxisArgs a) {
   using C = typename cplx_of<Real>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int N = a.min.n;
   const int G = N / E;
   const int W = blockDim.x / G;
+  const int wsh = __ffs(W) - 1;
   const int LD = line_ld(N);
-  C* sm = reinterpret_cast<C*>(smraw);
-  long long* cin = reinterpret_cast<long long*>(sm + (size_t)W * LD);
+  const int f = blockIdx.y;
+  const int ntile = (MODE == 1) ? 2 : 1;
+  C* t1 = reinterpret_cast<C*>(smraw);
+  C* t2 = t1 + (size_t)W * LD;
+  long long* cin = reinterpret_cast<long long*>(t1 + (size_t)ntile * W * LD);
   long long* cout = cin + W;
   Real* ck = reinterpret_cast<Real*>(cout + W);  // k1, kz per column (curl)
-  const int f = blockIdx.y;
   const long long l0 = (long long)blockIdx.x * W;
   const int tid = threadIdx.x, nth = blockDim.x;
 
@@ -57,62 +74,94 @@ __global__ void __launch_bounds__(256) k_axis(AxisArgs a) {
   }
   __syncthreads();
 
+  // inputs: MODE 0 field f; MODE 1 curl fields read two components
+  int c1 = f, c2 = -1;
+  if (MODE == 1) {
+    if (f == 3) { c1 = 2; c2 = 1; }       // i (k1 uz - kz uy)
+    else if (f == 4) { c1 = 0; c2 = 2; }  // i (kz ux - k0 uz)
+    else if (f == 5) { c1 = 1; c2 = 0; }  // i (k0 uy - k1 ux)
+  }
   const int rin = a.min.rows();
   const C* in = reinterpret_cast<const C*>(a.in);
-  for (int i = tid; i < rin * W; i += nth) {
-    const int r = i / W, w = i - r * W;
-    const long long bi = cin[w];
-    C v = czero<C>();
-    if (bi >= 0) {
-      if (MODE == 0) {
-        v = in[f * a.in_fs + r * a.in_rs + bi];
-      } else {
+  {
+    const C* s1 = in + c1 * a.in_fs;
+    const C* s2 = in + (c2 >= 0 ? c2 : 0) * a.in_fs;
+    for (int i = tid; i < rin * W; i += nth) {
+      const int r = i >> wsh, w = i & (W - 1);
+      const long long bi = cin[w];
+      if (bi >= 0) {
         const long long o = r * a.in_rs + bi;
-        if (f < 3) {
-          v = in[f * a.in_fs + o];
-        } else {
-          const Real k0 = (Real)(a.kscale[0] * a.min.wave(r));
-          const Real k1 = ck[2 * w], k2 = ck[2 * w + 1];
-          C t;
-          if (f == 3) {        // i (k1 uz - kz uy)
-            const C uy = in[1 * a.in_fs + o], uz = in[2 * a.in_fs + o];
-            t = mk<C>(k1 * uz.x - k2 * uy.x, k1 * uz.y - k2 * uy.y);
-          } else if (f == 4) { // i (kz ux - k0 uz)
-            const C ux = in[o], uz = in[2 * a.in_fs + o];
-            t = mk<C>(k2 * ux.x - k0 * uz.x, k2 * ux.y - k0 * uz.y);
-          } else {             // i (k0 uy - k1 ux)
-            const C ux = in[o], uy = in[1 * a.in_fs + o];
-            t = mk<C>(k0 * uy.x - k1 * ux.x, k0 * uy.y - k1 * ux.y);
-          }
-          v = mk<C>(-t.y, t.x);
-        }
+        cp_async<sizeof(C)>(&t1[w * LD + padp(r)], s1 + o);
+        if (c2 >= 0) cp_async<sizeof(C)>(&t2[w * LD + padp(r)], s2 + o);
       }
     }
-    sm[w * LD + padp(a.min.pos(r))] = v;
-  }
-  if (a.min.kc >= 0) {
-    const int nz = N - rin;
-    for (int i = tid; i < nz * W; i += nth) {
-      const int q = i / W, w = i - q * W;
-      sm[w * LD + padp(a.min.kc + 1 + q)] = czero<C>();
-    }
+    cp_commit();
+    cp_wait_all();
   }
   __syncthreads();
   {
     const int lane = tid & 31, warp = tid >> 5;
     const int w = warp * (32 / G) + lane / G;
-    line_fft<E, S>(sm + w * LD, lane % G, N, reinterpret_cast<const C*>(a.tw));
+    C* line = t1 + w * LD;
+    const C* line2 = t2 + w * LD;
+    const RowMap mi = a.min;
+    const Real k1 = (MODE == 1) ? ck[2 * w] : (Real)0, kz = (MODE == 1) ? ck[2 * w + 1] : (Real)0;
+    const Real ks0 = (Real)a.kscale[0];
+    const int fm = f;
+    auto ld = [&](int p) -> C {
+      int r = p;
+      if (mi.kc >= 0) {
+        if (p > mi.kc && p < N - mi.kc) return czero<C>();
+        if (p > mi.kc) r = p - N + 2 * mi.kc + 1;
+      }
+      const C v1 = line[padp(r)];
+      if (MODE == 0 || fm < 3) return v1;
+      const C v2 = line2[padp(r)];
+      C t;
+      if (fm == 3) {
+        t = mk<C>(k1 * v1.x - kz * v2.x, k1 * v1.y - kz * v2.y);
+      } else {
+        const Real k0 = ks0 * (Real)mi.wave(r);
+        if (fm == 4) t = mk<C>(kz * v1.x - k0 * v2.x, kz * v1.y - k0 * v2.y);
+        else t = mk<C>(k0 * v1.x - k1 * v2.x, k0 * v1.y - k1 * v2.y);
+      }
+      return mk<C>(-t.y, t.x);
+    };
+    line_fft_ld<E, S>(line, lane % G, N, reinterpret_cast<const C*>(a.tw), ld);
   }
   __syncthreads();
   const int rout = a.mout.rows();
-  C* out = reinterpret_cast<C*>(a.out);
+  C* out = reinterpret_cast<C*>(a.out) + f * a.out_fs;
   const Real sc = (Real)a.scale;
-  for (int i = tid; i < rout * W; i += nth) {
-    const int r = i / W, w = i - r * W;
-    const long long bo = cout[w];
-    if (bo >= 0) {
-      const C v = sm[w * LD + padp(a.mout.pos(r))];
-      out[f * a.out_fs + r * a.out_rs + bo] = mk<C>(v.x * sc, v.y * sc);
+  if (sizeof(C) == 8) {
+    // pairs of adjacent lines -> one 16-byte store
+    const int Wh = W >> 1;
+    for (int i = tid; i < rout * Wh; i += nth) {
+      const int r = i / Wh, w = (i - r * Wh) * 2;
+      const long long b0 = cout[w], b1 = cout[w + 1];
+      if (b0 < 0) continue;
+      const int pp = padp(a.mout.pos(r));
+      const C v0 = t1[w * LD + pp];
+      const long long o = r * a.out_rs + b0;
+      if (b1 == b0 + 1 && ((o & 1) == 0)) {
+        const C v1 = t1[(w + 1) * LD + pp];
+        reinterpret_cast<float4*>(out)[o >> 1] = make_float4(v0.x * sc, v0.y * sc, v1.x * sc, v1.y * sc);
+      } else {
+        out[o] = mk<C>(v0.x * sc, v0.y * sc);
+        if (b1 >= 0) {
+          const C v1 = t1[(w + 1) * LD + pp];
+          out[r * a.out_rs + b1] = mk<C>(v1.x * sc, v1.y * sc);
+        }
+      }
+    }
+  } else {
+    for (int i = tid; i < rout * W; i += nth) {
+      const int r = i >> wsh, w = i & (W - 1);
+      const long long bo = cout[w];
+      if (bo >= 0) {
+        const C v = t1[w * LD + padp(a.mout.pos(r))];
+        out[r * a.out_rs + bo] = mk<C>(v.x * sc, v.y * sc);
+      }
     }
   }
 }
@@ -135,7 +184,113 @@ __device__ __forceinline__ void pack_pair(C* cb, const C* pa, const C* pb, int K
   for (int q = Kz + g; q <= n - Kz; q += G) cb[padp(q)] = czero<C>();
 }
 
-// MODE 0: NS (6 fields -> cross -> 3 fields), 1: C2R only, 2: R2C only
+// extract the half spectra of the two real lines packed in X (forward FFT of a + i b)
+template <typename C, typename Real>
+__device__ __forceinline__ void unpack_pair(const C* buf, int kz, int N, C& oa, C& ob) {
+  const C X = buf[padp(kz)];
+  const C Yc = buf[padp((N - kz) & (N - 1))];
+  oa = mk<C>((Real)0.5 * (X.x + Yc.x), (Real)0.5 * (X.y - Yc.y));
+  ob = mk<C>((Real)0.5 * (X.y + Yc.y), (Real)0.5 * (Yc.x - X.x));
+}
+
+// Fused NS z sweep (persistent warps).  Per line: stage the 6 spectral rows
+// (u_hat, w_hat after the x and y inverse sweeps) with cp.async, pack pairs,
+// 3 inverse FFTs, u x w (+ CFL maximum), 2 forward FFTs, store 3 rows.  The
+// staging area is refilled with the next line while the current one is
+// transformed.
+// complex values of shared memory per warp of k_zline_ns (kept even so that
+// every warp block starts on a 16-byte boundary)
+__host__ __device__ inline size_t zns_per_warp(int LD, int Kzp, int LPW) {
+  const size_t n = (size_t)LPW * ((size_t)6 * Kzp + (size_t)3 * LD);
+  return (n + 1) & ~(size_t)1;
+}
+
+template <typename Real, int E>
+__global__ void __launch_bounds__(64) k_zline_ns(ZArgs a) {
+  using C = typename cplx_of<Real>::type;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const int N = a.n, G = N / E, LPW = 32 / G, LD = line_ld(N);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / G, g = lane % G;
+  const int Kzp = a.Kzp;
+  // per warp: LPW staging areas of 6 rows of Kzp (16-byte aligned: Kzp is a
+  // multiple of 8 and each warp block has an even number of complex values),
+  // then LPW x 3 work buffers of LD
+  const size_t per_warp = zns_per_warp(LD, Kzp, LPW);
+  C* base = sm + (size_t)warp * per_warp;
+  C* stg = base + (size_t)sub * 6 * Kzp;
+  C* buf = base + (size_t)LPW * 6 * Kzp + (size_t)sub * 3 * LD;
+  const C* tw = reinterpret_cast<const C*>(a.tw);
+  const long long fs = a.nlines * Kzp;
+  const C* in = reinterpret_cast<const C*>(a.in);
+  C* out = reinterpret_cast<C*>(a.out);
+  const long long wstride = (long long)gridDim.x * (blockDim.x >> 5) * LPW;
+  const long long wfirst = ((long long)blockIdx.x * (blockDim.x >> 5) + warp) * LPW;
+  long long line = wfirst + sub;
+  constexpr int VB = 16 / (int)sizeof(C);  // complex values per 16-byte copy
+  auto stage = [&](long long ln) {
+    if (ln < a.nlines) {
+      const int nchunk = 6 * Kzp / VB;
+      for (int q = g; q < nchunk; q += G) {
+        const int f = (q * VB) / Kzp, k = q * VB - f * Kzp;
+        cp_async16(stg + f * Kzp + k, in + f * fs + ln * Kzp + k);
+      }
+    }
+    cp_commit();
+  };
+  stage(line);
+  double rmax = 0.0;
+  // all lanes of a warp iterate together (the loop bound is the warp's first line)
+  for (long long wl = wfirst; wl < a.nlines; wl += wstride, line += wstride) {
+    const bool valid = line < a.nlines;
+    cp_wait_all();
+    __syncwarp();
+    // pack 3 pairs from staging into the work buffers
+    for (int p = 0; p < 3; ++p)
+      pack_pair(buf + p * LD, stg + (2 * p) * Kzp, stg + (2 * p + 1) * Kzp, a.Kz, N, g, G, valid);
+    __syncwarp();
+    stage(line + wstride);
+    for (int p = 0; p < 3; ++p) line_fft<E, +1>(buf + p * LD, g, N, tw);
+#pragma unroll 4
+    for (int m = 0; m < E; ++m) {
+      const int n = padp(g + G * m);
+      const C c0 = buf[n], c1 = buf[LD + n], c2 = buf[2 * LD + n];
+      const Real u0 = c0.x, u1 = c0.y, u2 = c1.x, w0 = c1.y, w1 = c2.x, w2 = c2.y;
+      if (a.cfl_rate && valid)
+        rmax = fmax(rmax, fabs((double)u0) * a.inv_dx[0] + fabs((double)u1) * a.inv_dx[1] +
+                              fabs((double)u2) * a.inv_dx[2]);
+      buf[n] = mk<C>(u1 * w2 - u2 * w1, u2 * w0 - u0 * w2);
+      buf[LD + n] = mk<C>(u0 * w1 - u1 * w0, (Real)0);
+    }
+    __syncwarp();
+    line_fft<E, -1>(buf, g, N, tw);
+    line_fft<E, -1>(buf + LD, g, N, tw);
+    if (valid) {
+      const long long lo = line * Kzp;
+      for (int kz = g; kz < Kzp; kz += G) {
+        C oa = czero<C>(), ob = czero<C>(), oc = czero<C>();
+        if (kz < a.Kz) {
+          unpack_pair<C, Real>(buf, kz, N, oa, ob);
+          oc = buf[LD + padp(kz)];
+        }
+        out[lo + kz] = oa;
+        out[fs + lo + kz] = ob;
+        out[2 * fs + lo + kz] = oc;
+      }
+    }
+    __syncwarp();
+  }
+  cp_wait_all();
+  if (a.cfl_rate) {
+    for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    if (lane == 0 && rmax > 0.0)
+      atomicMax(reinterpret_cast<unsigned long long*>(a.cfl_rate), (unsigned long long)__double_as_longlong(rmax));
+  }
+}
+
+// C2R-only (MODE 1) and R2C-only (MODE 2) z sweeps of the unpruned
+// diagnostic transforms (not on the RK4 path).
 template <typename Real, int E, int MODE>
 __global__ void __launch_bounds__(128) k_zline(ZArgs a) {
   using C = typename cplx_of<Real>::type;
@@ -146,27 +301,22 @@ __global__ void __launch_bounds__(128) k_zline(ZArgs a) {
   const int sub = lane / G, g = lane % G;
   const long long line = ((long long)blockIdx.x * (blockDim.x >> 5) + warp) * LPW + sub;
   const bool valid = line < a.nlines;
-  const int NB = (MODE == 0) ? 3 : 2;
-  C* buf = sm + (size_t)((warp * LPW + sub) * NB) * LD;
+  C* buf = sm + (size_t)((warp * LPW + sub) * 2) * LD;
   const C* tw = reinterpret_cast<const C*>(a.tw);
   const long long fs = a.nlines * a.Kzp;
-  const C* in = reinterpret_cast<const C*>(a.in);
   const long long lo = line * a.Kzp;
-  const int npair = (MODE == 0) ? 3 : (a.nf + 1) / 2;
-
-  if (MODE == 0 || MODE == 1) {
+  const int npair = (a.nf + 1) / 2;
+  const long long pfs = a.nlines * (long long)N;
+  if (MODE == 1) {
+    const C* in = reinterpret_cast<const C*>(a.in);
     for (int p = 0; p < npair; ++p) {
-      const int fa = 2 * p, fb = 2 * p + 1;
-      const int nfin = (MODE == 0) ? 6 : a.nf;
-      pack_pair(buf + p * LD, in + fa * fs + lo, fb < nfin ? in + fb * fs + lo : (const C*)nullptr,
-                a.Kz, N, g, G, valid);
+      const int fb = 2 * p + 1;
+      pack_pair(buf + p * LD, in + (2 * p) * fs + lo, fb < a.nf ? in + fb * fs + lo : (const C*)nullptr, a.Kz, N, g,
+                G, valid);
     }
     __syncwarp();
     for (int p = 0; p < npair; ++p) line_fft<E, +1>(buf + p * LD, g, N, tw);
-  }
-  if (MODE == 1) {
     Real* ph = reinterpret_cast<Real*>(a.phys);
-    const long long pfs = a.nlines * (long long)N;
     if (valid) {
       for (int m = 0; m < E; ++m) {
         const int n = g + G * m;
@@ -179,57 +329,29 @@ __global__ void __launch_bounds__(128) k_zline(ZArgs a) {
     }
     return;
   }
-  if (MODE == 0) {
-    double rmax = 0.0;
-#pragma unroll 4
+  const Real* ph = reinterpret_cast<const Real*>(a.phys);
+  for (int p = 0; p < npair; ++p) {
     for (int m = 0; m < E; ++m) {
-      const int n = padp(g + G * m);
-      const C c0 = buf[n], c1 = buf[LD + n], c2 = buf[2 * LD + n];
-      const Real u0 = c0.x, u1 = c0.y, u2 = c1.x, w0 = c1.y, w1 = c2.x, w2 = c2.y;
-      if (a.cfl_rate)
-        rmax = fmax(rmax, fabs((double)u0) * a.inv_dx[0] + fabs((double)u1) * a.inv_dx[1] + fabs((double)u2) * a.inv_dx[2]);
-      buf[n] = mk<C>(u1 * w2 - u2 * w1, u2 * w0 - u0 * w2);
-      buf[LD + n] = mk<C>(u0 * w1 - u1 * w0, (Real)0);
-    }
-    if (a.cfl_rate) {
-      if (!valid) rmax = 0.0;
-      for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
-      if (lane == 0) atomicMax(reinterpret_cast<unsigned long long*>(a.cfl_rate), (unsigned long long)__double_as_longlong(rmax));
-    }
-  } else {  // MODE 2: load physical pairs
-    const Real* ph = reinterpret_cast<const Real*>(a.phys);
-    const long long pfs = a.nlines * (long long)N;
-    for (int p = 0; p < npair; ++p) {
-      for (int m = 0; m < E; ++m) {
-        const int n = g + G * m;
-        Real x = 0, y = 0;
-        if (valid) {
-          x = ph[(2 * p) * pfs + line * N + n];
-          if (2 * p + 1 < a.nf) y = ph[(2 * p + 1) * pfs + line * N + n];
-        }
-        buf[p * LD + padp(n)] = mk<C>(x, y);
+      const int n = g + G * m;
+      Real x = 0, y = 0;
+      if (valid) {
+        x = ph[(2 * p) * pfs + line * N + n];
+        if (2 * p + 1 < a.nf) y = ph[(2 * p + 1) * pfs + line * N + n];
       }
+      buf[p * LD + padp(n)] = mk<C>(x, y);
     }
   }
   __syncwarp();
-  const int nout = (MODE == 0) ? 3 : a.nf;
-  const int nfwd = (nout + 1) / 2;
-  for (int p = 0; p < nfwd; ++p) line_fft<E, -1>(buf + p * LD, g, N, tw);
+  for (int p = 0; p < npair; ++p) line_fft<E, -1>(buf + p * LD, g, N, tw);
   if (!valid) return;
   C* out = reinterpret_cast<C*>(a.out);
   for (int kz = g; kz < a.Kzp; kz += G) {
-    for (int p = 0; p < nfwd; ++p) {
-      const bool two = (2 * p + 1 < nout);
+    for (int p = 0; p < npair; ++p) {
+      const bool two = (2 * p + 1 < a.nf);
       C oa = czero<C>(), ob = czero<C>();
       if (kz < a.Kz) {
-        const C X = buf[p * LD + padp(kz)];
-        if (two) {
-          const C Yc = buf[p * LD + padp((N - kz) & (N - 1))];
-          oa = mk<C>((Real)0.5 * (X.x + Yc.x), (Real)0.5 * (X.y - Yc.y));
-          ob = mk<C>((Real)0.5 * (X.y + Yc.y), (Real)0.5 * (Yc.x - X.x));
-        } else {
-          oa = X;
-        }
+        if (two) unpack_pair<C, Real>(buf + p * LD, kz, N, oa, ob);
+        else oa = buf[p * LD + padp(kz)];
       }
       out[(2 * p) * fs + lo + kz] = oa;
       if (two) out[(2 * p + 1) * fs + lo + kz] = ob;
@@ -238,19 +360,21 @@ __global__ void __launch_bounds__(128) k_zline(ZArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// final x sweep + projection + diffusion + source + RK4 stage update
+// final x sweep + projection + diffusion + source + RK4 stage update.
+// Single solver: right-hand side in FP32, S and A float-float (compensated);
+// double solver: FP64 throughout.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double2 d2(double x, double y) { return make_double2(x, y); }
-
 template <typename Real, int E>
-__global__ void __launch_bounds__(256) k_axis_rk(RKArgs a) {
+__global__ void __launch_bounds__(256, 2) k_axis_rk(RKArgs a) {
   using C = typename cplx_of<Real>::type;
+  using AT = typename Acc<Real>::T;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int N = a.m0.n, G = N / E, W = blockDim.x / G, LD = line_ld(N);
+  const int wsh = __ffs(W) - 1;
   C* sm = reinterpret_cast<C*>(smraw);
   int* ck1 = reinterpret_cast<int*>(sm + (size_t)3 * W * LD);
   int* ckz = ck1 + W;
-  __shared__ double red[2][32];
+  __shared__ double red[2][8];
   const long long l0 = (long long)blockIdx.x * W;
   const int tid = threadIdx.x, nth = blockDim.x;
   const long long nl = a.nlines;
@@ -266,19 +390,23 @@ __global__ void __launch_bounds__(256) k_axis_rk(RKArgs a) {
     }
   }
   const C* in = reinterpret_cast<const C*>(a.in);
-  for (int f = 0; f < 3; ++f) {
-    for (int i = tid; i < N * W; i += nth) {
-      const int r = i / W, w = i - r * W;
-      const long long l = l0 + w;
-      sm[(f * W + w) * LD + padp(r)] = (l < nl) ? in[((long long)f * N + r) * nl + l] : czero<C>();
-    }
+  for (int i = tid; i < 3 * N * W; i += nth) {
+    const int w = i & (W - 1), fr = i >> wsh, f = fr / N, r = fr - f * N;
+    const long long l = l0 + w;
+    if (l < nl) cp_async<sizeof(C)>(&sm[(f * W + w) * LD + padp(r)], in + ((long long)f * N + r) * nl + l);
   }
+  cp_commit();
+  cp_wait_all();
   __syncthreads();
   {
     const int lane = tid & 31, warp = tid >> 5;
     const int w = warp * (32 / G) + lane / G;
     const C* tw = reinterpret_cast<const C*>(a.tw);
-    for (int f = 0; f < 3; ++f) line_fft<E, -1>(sm + (f * W + w) * LD, lane % G, N, tw);
+    for (int f = 0; f < 3; ++f) {
+      C* line = sm + (f * W + w) * LD;
+      auto ld = [&](int p) -> C { return line[padp(p)]; };
+      line_fft_ld<E, -1>(line, lane % G, N, tw, ld);
+    }
   }
   __syncthreads();
 
@@ -287,80 +415,116 @@ __global__ void __launch_bounds__(256) k_axis_rk(RKArgs a) {
   const double dt = *a.dt;
   const double alpha = a.force_alpha ? *a.force_alpha : 0.0;
   C* Y = reinterpret_cast<C*>(a.Y);
+  AT* Sg = reinterpret_cast<AT*>(a.S);
+  AT* Ag = reinterpret_cast<AT*>(a.A);
+  const AT* src = reinterpret_cast<const AT*>(a.source);
+  const Real sc = (Real)a.scale;
+  const Real ks0 = (Real)a.kscale[0], ks1 = (Real)a.kscale[1], ks2 = (Real)a.kscale[2];
+  const Real nu = (Real)a.nu;
+  const Real bdt = (Real)(a.b * dt), adt = (Real)(a.a * dt), alph = (Real)alpha;
+  const Real kf2 = (Real)a.kf2;
   double e_sum = 0.0, z_sum = 0.0;
   for (int i = tid; i < K0 * W; i += nth) {
-    const int r = i / W, w = i - r * W;
+    const int r = i >> wsh, w = i & (W - 1);
     const int k1row = ck1[w], kz = ckz[w];
     if (k1row < 0) continue;
     const long long o = (long long)r * nl + l0 + w;
     if (kz >= a.Kz) {  // padding of the R2C axis stays zero
+      AT z0;
+      memset(&z0, 0, sizeof(z0));
       for (int c = 0; c < 3; ++c) {
         if (a.stage == 4) {
           reinterpret_cast<C*>(a.rhs_out)[c * cs + o] = czero<C>();
         } else {
           Y[c * cs + o] = czero<C>();
-          if (a.stage == 3) a.S[c * cs + o] = d2(0, 0); else a.A[c * cs + o] = d2(0, 0);
+          if (a.stage == 3) Sg[c * cs + o] = z0; else Ag[c * cs + o] = z0;
         }
       }
       if (a.p_out) reinterpret_cast<C*>(a.p_out)[o] = czero<C>();
       continue;
     }
     const int p = a.m0.pos(r);
-    const double k[3] = {a.kscale[0] * a.m0.wave(r), a.kscale[1] * a.m1.wave(k1row), a.kscale[2] * kz};
-    const double K2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
-    const double iK2 = K2 > 0.0 ? 1.0 / K2 : 0.0;
-    double2 nlv[3];
+    const Real k[3] = {ks0 * (Real)a.m0.wave(r), ks1 * (Real)a.m1.wave(k1row), ks2 * (Real)kz};
+    const Real K2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+    const Real iK2 = K2 > (Real)0 ? (Real)1 / K2 : (Real)0;
+    C nlv[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const C v = sm[(c * W + w) * LD + padp(p)];
-      nlv[c] = d2((double)v.x * a.scale, (double)v.y * a.scale);
+      nlv[c] = mk<C>(v.x * sc, v.y * sc);
     }
-    const double2 P = d2((nlv[0].x * k[0] + nlv[1].x * k[1] + nlv[2].x * k[2]) * iK2,
-                         (nlv[0].y * k[0] + nlv[1].y * k[1] + nlv[2].y * k[2]) * iK2);
-    if (a.p_out) reinterpret_cast<C*>(a.p_out)[o] = mk<C>((Real)P.x, (Real)P.y);
-    const bool forced = a.force_alpha && K2 > 0.0 && K2 <= a.kf2;
-    double2 snew[3];
+    const C P = mk<C>((nlv[0].x * k[0] + nlv[1].x * k[1] + nlv[2].x * k[2]) * iK2,
+                      (nlv[0].y * k[0] + nlv[1].y * k[1] + nlv[2].y * k[2]) * iK2);
+    if (a.p_out) reinterpret_cast<C*>(a.p_out)[o] = P;
+    const bool forced = a.force_alpha && K2 > (Real)0 && K2 <= kf2;
+    const Real nuK2 = nu * K2;
+    Real snx[3] = {0, 0, 0}, sny[3] = {0, 0, 0};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const long long oc = c * cs + o;
-      double2 u, s;
-      if (a.stage == 0) {
-        s = a.S[oc];
-        u = s;
-      } else {
-        const C y = Y[oc];
-        u = d2((double)y.x, (double)y.y);
-        if (a.stage == 1 || a.stage == 2 || forced) s = a.S[oc];
-      }
-      double2 rhs = d2(nlv[c].x - P.x * k[c] - a.nu * K2 * u.x, nlv[c].y - P.y * k[c] - a.nu * K2 * u.y);
-      if (a.source) { const double2 q = a.source[oc]; rhs.x += q.x; rhs.y += q.y; }
-      if (forced) { rhs.x += alpha * s.x; rhs.y += alpha * s.y; }
+      AT s, acc;
+      memset(&s, 0, sizeof(s));
+      C u;
+      const bool need_s = a.stage == 0 || a.stage == 1 || a.stage == 2 || forced;
+      if (need_s) s = Sg[oc];
+      if (a.stage == 0) u = mk<C>((Real)s.x, (Real)s.y);
+      else u = Y[oc];
+      C rhs = mk<C>(nlv[c].x - P.x * k[c] - nuK2 * u.x, nlv[c].y - P.y * k[c] - nuK2 * u.y);
+      if (src) { const AT q = src[oc]; rhs.x += (Real)q.x; rhs.y += (Real)q.y; }
+      if (forced) { rhs.x += alph * (Real)s.x; rhs.y += alph * (Real)s.y; }
       if (a.stage == 4) {
-        reinterpret_cast<C*>(a.rhs_out)[oc] = mk<C>((Real)rhs.x, (Real)rhs.y);
-      } else if (a.stage == 0) {
-        Y[oc] = mk<C>((Real)(s.x + a.b * dt * rhs.x), (Real)(s.y + a.b * dt * rhs.y));
-        a.A[oc] = d2(s.x + a.a * dt * rhs.x, s.y + a.a * dt * rhs.y);
-      } else if (a.stage < 3) {
-        const double2 acc = a.A[oc];
-        Y[oc] = mk<C>((Real)(s.x + a.b * dt * rhs.x), (Real)(s.y + a.b * dt * rhs.y));
-        a.A[oc] = d2(acc.x + a.a * dt * rhs.x, acc.y + a.a * dt * rhs.y);
+        reinterpret_cast<C*>(a.rhs_out)[oc] = rhs;
+        continue;
+      }
+      if constexpr (sizeof(Real) == 4) {
+        // compensated FP32: Y' = S + b dt rhs ; A' = (S or A) + a dt rhs
+        if (a.stage < 3) {
+          float yx = s.x, ylx = s.z, yy = s.y, yly = s.w;
+          ff_add(yx, ylx, bdt * rhs.x);
+          ff_add(yy, yly, bdt * rhs.y);
+          Y[oc] = mk<C>(yx, yy);
+          if (a.stage == 0) acc = s; else acc = Ag[oc];
+          ff_add(acc.x, acc.z, adt * rhs.x);
+          ff_add(acc.y, acc.w, adt * rhs.y);
+          Ag[oc] = acc;
+        } else {
+          acc = Ag[oc];
+          ff_add(acc.x, acc.z, adt * rhs.x);
+          ff_add(acc.y, acc.w, adt * rhs.y);
+          Sg[oc] = acc;
+          Y[oc] = mk<C>(acc.x, acc.y);
+          snx[c] = acc.x;
+          sny[c] = acc.y;
+        }
       } else {
-        const double2 acc = a.A[oc];
-        const double2 sn = d2(acc.x + a.a * dt * rhs.x, acc.y + a.a * dt * rhs.y);
-        a.S[oc] = sn;
-        Y[oc] = mk<C>((Real)sn.x, (Real)sn.y);
-        snew[c] = sn;
+        const double bd = a.b * dt, ad = a.a * dt;
+        if (a.stage < 3) {
+          Y[oc] = mk<C>(s.x + bd * rhs.x, s.y + bd * rhs.y);
+          if (a.stage == 0) acc = s; else acc = Ag[oc];
+          acc.x += ad * rhs.x;
+          acc.y += ad * rhs.y;
+          Ag[oc] = acc;
+        } else {
+          acc = Ag[oc];
+          acc.x += ad * rhs.x;
+          acc.y += ad * rhs.y;
+          Sg[oc] = acc;
+          Y[oc] = mk<C>(acc.x, acc.y);
+          snx[c] = (Real)acc.x;
+          sny[c] = (Real)acc.y;
+        }
       }
     }
     if (a.stage == 3) {
-      const double wz = (kz == 0) ? 0.5 : 1.0;  // 1/2 * Hermitian weight
-      e_sum += wz * (snew[0].x * snew[0].x + snew[0].y * snew[0].y + snew[1].x * snew[1].x +
-                     snew[1].y * snew[1].y + snew[2].x * snew[2].x + snew[2].y * snew[2].y);
-      // |k x u|^2
-      const double cx_r = k[1] * snew[2].x - k[2] * snew[1].x, cx_i = k[1] * snew[2].y - k[2] * snew[1].y;
-      const double cy_r = k[2] * snew[0].x - k[0] * snew[2].x, cy_i = k[2] * snew[0].y - k[0] * snew[2].y;
-      const double cz_r = k[0] * snew[1].x - k[1] * snew[0].x, cz_i = k[0] * snew[1].y - k[1] * snew[0].y;
-      z_sum += wz * (cx_r * cx_r + cx_i * cx_i + cy_r * cy_r + cy_i * cy_i + cz_r * cz_r + cz_i * cz_i);
+      const Real wz = (kz == 0) ? (Real)0.5 : (Real)1;  // 1/2 * Hermitian weight
+      const Real e = snx[0] * snx[0] + sny[0] * sny[0] + snx[1] * snx[1] + sny[1] * sny[1] + snx[2] * snx[2] +
+                     sny[2] * sny[2];
+      const Real cxr = k[1] * snx[2] - k[2] * snx[1], cxi = k[1] * sny[2] - k[2] * sny[1];
+      const Real cyr = k[2] * snx[0] - k[0] * snx[2], cyi = k[2] * sny[0] - k[0] * sny[2];
+      const Real czr = k[0] * snx[1] - k[1] * snx[0], czi = k[0] * sny[1] - k[1] * sny[0];
+      const Real z = cxr * cxr + cxi * cxi + cyr * cyr + cyi * cyi + czr * czr + czi * czi;
+      e_sum += (double)(wz * e);
+      z_sum += (double)(wz * z);
     }
   }
   if (a.stage == 3 && a.partials) {
@@ -388,7 +552,8 @@ inline int elems_for(int n) { return n >= 1024 ? 32 : 16; }
 template <typename Real>
 static size_t axis_smem(int n, int W, bool curl) {
   using C = typename cplx_of<Real>::type;
-  return (size_t)W * line_ld(n) * sizeof(C) + 2 * W * sizeof(long long) + (curl ? 2 * W * sizeof(Real) : 0) + 16;
+  return (size_t)(curl ? 2 : 1) * W * line_ld(n) * sizeof(C) + 2 * W * sizeof(long long) +
+         (curl ? 2 * W * sizeof(Real) : 0) + 16;
 }
 
 template <typename Real, int E, int S, int MODE>
@@ -416,13 +581,32 @@ int Kernels<Real>::axis_curl_inv(const AxisArgs& a, cudaStream_t s) {
   return launch_axis<Real, 32, 1, 1>(a, s);
 }
 
+template <typename Real, int E>
+static int launch_zns(const ZArgs& a, cudaStream_t s) {
+  using C = typename cplx_of<Real>::type;
+  const int G = a.n / E, LPW = 32 / G;
+  const int warps = 2;
+  if (a.Kzp % 8 != 0) return (int)cudaErrorInvalidValue;  // 16-byte staging copies need Kzp % 8 == 0
+  const size_t sm = (size_t)warps * zns_per_warp(line_ld(a.n), a.Kzp, LPW) * sizeof(C);
+  auto kern = k_zline_ns<Real, E>;
+  int dev = 0, nsm = 148, occ = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, warps * 32, sm);
+  if (occ < 1) occ = 1;
+  const long long per_block = (long long)warps * LPW;
+  long long nb = (a.nlines + per_block - 1) / per_block;
+  if (nb > (long long)occ * nsm) nb = (long long)occ * nsm;
+  kern<<<(unsigned)nb, warps * 32, sm, s>>>(a);
+  return (int)cudaGetLastError();
+}
+
 template <typename Real, int E, int MODE>
 static int launch_z(const ZArgs& a, cudaStream_t s) {
   using C = typename cplx_of<Real>::type;
   const int G = a.n / E, LPW = 32 / G;
-  const int NB = (MODE == 0) ? 3 : 2;
   const int warps = 4;
-  const size_t sm = (size_t)warps * LPW * NB * line_ld(a.n) * sizeof(C);
+  const size_t sm = (size_t)warps * LPW * 2 * line_ld(a.n) * sizeof(C);
   auto kern = k_zline<Real, E, MODE>;
   const long long per_block = (long long)warps * LPW;
   dim3 grid((unsigned)((a.nlines + per_block - 1) / per_block));
@@ -432,7 +616,7 @@ static int launch_z(const ZArgs& a, cudaStream_t s) {
 
 template <typename Real>
 int Kernels<Real>::zline_ns(const ZArgs& a, cudaStream_t s) {
-  return elems_for(a.n) == 16 ? launch_z<Real, 16, 0>(a, s) : launch_z<Real, 32, 0>(a, s);
+  return elems_for(a.n) == 16 ? launch_zns<Real, 16>(a, s) : launch_zns<Real, 32>(a, s);
 }
 template <typename Real>
 int Kernels<Real>::zline_c2r(const ZArgs& a, cudaStream_t s) {
@@ -443,14 +627,20 @@ int Kernels<Real>::zline_r2c(const ZArgs& a, cudaStream_t s) {
   return elems_for(a.n) == 16 ? launch_z<Real, 16, 2>(a, s) : launch_z<Real, 32, 2>(a, s);
 }
 
+// tile width (lines) of the RK sweep for an axis of n0 points
+inline int rk_width(int n0, size_t csz) {
+  const int E = elems_for(n0), G = n0 / E;
+  int W = 256 / G;
+  while (W > 1 && (size_t)3 * W * line_ld(n0) * csz + 2 * W * sizeof(int) + 16 > 200 * 1024) W /= 2;
+  return W;
+}
+
 template <typename Real, int E>
 static int launch_rk(const RKArgs& a, cudaStream_t s, int* nblocks) {
   using C = typename cplx_of<Real>::type;
   const int G = a.m0.n / E;
-  int W = 256 / G;
-  auto smsize = [&](int w) { return (size_t)3 * w * line_ld(a.m0.n) * sizeof(C) + 2 * w * sizeof(int) + 16; };
-  while (W > 1 && smsize(W) > 200 * 1024) W /= 2;
-  const size_t sm = smsize(W);
+  const int W = rk_width(a.m0.n, sizeof(C));
+  const size_t sm = (size_t)3 * W * line_ld(a.m0.n) * sizeof(C) + 2 * W * sizeof(int) + 16;
   auto kern = k_axis_rk<Real, E>;
   const unsigned nb = (unsigned)((a.nlines + W - 1) / W);
   if (nblocks) *nblocks = (int)nb;
@@ -463,8 +653,6 @@ int Kernels<Real>::axis_rk(const RKArgs& a, cudaStream_t s, int* nblocks) {
   return elems_for(a.m0.n) == 16 ? launch_rk<Real, 16>(a, s, nblocks) : launch_rk<Real, 32>(a, s, nblocks);
 }
 
-// Allow the large dynamic shared-memory tiles once per device (outside any
-// stream capture).
 template <typename K> static cudaError_t optin_one(K kern, int optin) {
   cudaFuncAttributes fa;
   cudaError_t e = cudaFuncGetAttributes(&fa, kern);
@@ -472,6 +660,8 @@ template <typename K> static cudaError_t optin_one(K kern, int optin) {
   return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
 }
 
+// Allow the large dynamic shared-memory tiles once per device (outside any
+// stream capture).
 template <typename Real>
 int Kernels<Real>::smem_optin(int dev) {
   int mx = 0;
@@ -479,21 +669,12 @@ int Kernels<Real>::smem_optin(int dev) {
 #define SDNS_OPT(k) if (e == cudaSuccess) e = optin_one(k, mx)
   SDNS_OPT((k_axis<Real, 16, -1, 0>)); SDNS_OPT((k_axis<Real, 16, 1, 0>)); SDNS_OPT((k_axis<Real, 16, 1, 1>));
   SDNS_OPT((k_axis<Real, 32, -1, 0>)); SDNS_OPT((k_axis<Real, 32, 1, 0>)); SDNS_OPT((k_axis<Real, 32, 1, 1>));
-  SDNS_OPT((k_zline<Real, 16, 0>)); SDNS_OPT((k_zline<Real, 16, 1>)); SDNS_OPT((k_zline<Real, 16, 2>));
-  SDNS_OPT((k_zline<Real, 32, 0>)); SDNS_OPT((k_zline<Real, 32, 1>)); SDNS_OPT((k_zline<Real, 32, 2>));
+  SDNS_OPT((k_zline_ns<Real, 16>)); SDNS_OPT((k_zline_ns<Real, 32>));
+  SDNS_OPT((k_zline<Real, 16, 1>)); SDNS_OPT((k_zline<Real, 16, 2>));
+  SDNS_OPT((k_zline<Real, 32, 1>)); SDNS_OPT((k_zline<Real, 32, 2>));
   SDNS_OPT((k_axis_rk<Real, 16>)); SDNS_OPT((k_axis_rk<Real, 32>));
 #undef SDNS_OPT
   return (int)e;
-}
-
-// number of CTAs axis_rk launches (for sizing the partials buffer)
-template <typename Real>
-inline long long rk_blocks(int n0, long long nlines) {
-  using C = typename cplx_of<Real>::type;
-  const int E = elems_for(n0), G = n0 / E;
-  int W = 256 / G;
-  while (W > 1 && (size_t)3 * W * line_ld(n0) * sizeof(C) + 2 * W * sizeof(int) + 16 > 200 * 1024) W /= 2;
-  return (nlines + W - 1) / W;
 }
 
 }  // namespace sdns
