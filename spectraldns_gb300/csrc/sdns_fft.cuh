@@ -216,6 +216,135 @@ __device__ __forceinline__ void line_fft_ld(C* buf, int g, int N, const C* __res
   }
 }
 
+// ---------------------------------------------------------------------------
+// Register-resident ends of a line transform.  After the last Stockham pass
+// the lane g of a group holds the outputs of positions g + G*m, m = 0..E-1,
+// in x[m]; the first radix-16 pass reads exactly the same positions.  A
+// transform can therefore start from, or end in, registers, and pointwise
+// work between an inverse and a forward transform needs no shared memory.
+// ---------------------------------------------------------------------------
+template <int R, int E, int S, typename C>
+__device__ __forceinline__ void last_pass_regs(const C* buf, int g, int G, int N, int Ns, const C* __restrict__ tw,
+                                               C (&x)[E]) {
+  constexpr int NB = E / R;
+  const int NR = N / R;
+  C v[E];
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const int j = g + G * q;
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[q * R + r] = buf[padp(j + r * NR)];
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const int j = g + G * q;  // j < Ns in the last pass, so (j mod Ns) = j
+#pragma unroll
+    for (int r = 1; r < R; ++r) {
+      C w = tw[r * Ns + j];
+      if (S > 0) w.y = -w.y;
+      v[q * R + r] = cmul(v[q * R + r], w);
+    }
+    dftR<R, S>(&v[q * R]);
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q)
+#pragma unroll
+    for (int r = 0; r < R; ++r) x[q + r * NB] = v[q * R + r];
+}
+
+// passes 2.. of a transform whose first pass has been written to `buf`;
+// the result ends in registers x[m] (position g + G*m)
+template <int E, int S, typename C>
+__device__ __forceinline__ void fft_tail_regs(C* buf, int g, int G, int N, const C* __restrict__ tw, C (&x)[E]) {
+  int Ns = 16, off = 16;
+  while (Ns * 16 < N) {
+    stockham_pass<16, E, S>(buf, g, G, N, Ns, tw + off);
+    off += 16 * Ns;
+    Ns *= 16;
+  }
+  switch (N / Ns) {
+    case 16: last_pass_regs<16, E, S>(buf, g, G, N, Ns, tw + off, x); break;
+    case 8: last_pass_regs<8, E, S>(buf, g, G, N, Ns, tw + off, x); break;
+    case 4: last_pass_regs<4, E, S>(buf, g, G, N, Ns, tw + off, x); break;
+    default: last_pass_regs<2, E, S>(buf, g, G, N, Ns, tw + off, x); break;
+  }
+}
+
+// transform with a loader-fed first pass, ending in registers (E == 16 when N == 16)
+template <int E, int S, typename C, typename Loader>
+__device__ __forceinline__ void fft_ld_regs(C* buf, int g, int N, const C* __restrict__ tw, Loader& ld, C (&x)[E]) {
+  const int G = N / E;
+  if (N == 16) {
+#pragma unroll
+    for (int r = 0; r < 16; ++r) x[r] = ld(r);
+    dft16<S>(x);
+    return;
+  }
+  stockham_first16<E, S>(buf, g, G, N, ld);
+  fft_tail_regs<E, S>(buf, g, G, N, tw, x);
+}
+
+// transform starting from registers x[m] (position g + G*m), ending in y[m]
+template <int E, int S, typename C>
+__device__ __forceinline__ void fft_regs_regs(C* buf, int g, int N, const C* __restrict__ tw, const C (&x)[E],
+                                              C (&y)[E]) {
+  const int G = N / E;
+  constexpr int NB = E / 16;
+  C v[E];
+#pragma unroll
+  for (int q = 0; q < NB; ++q)
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[q * 16 + r] = x[q + r * NB];
+#pragma unroll
+  for (int q = 0; q < NB; ++q) dft16<S>(&v[q * 16]);
+  if (N == 16) {
+#pragma unroll
+    for (int r = 0; r < E; ++r) y[r] = v[r];
+    return;
+  }
+  __syncwarp();  // earlier readers of buf are done
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const int j = g + G * q;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) buf[padp(j * 16 + r)] = v[q * 16 + r];
+  }
+  __syncwarp();
+  fft_tail_regs<E, S>(buf, g, G, N, tw, y);
+}
+
+// ---------------------------------------------------------------------------
+// Forward transform of a line of compile-time length N (16..512, E = 16)
+// held in registers: x[m] is position g + G*m on entry and holds the output
+// of position g + G*m on exit.  The pass structure is fixed at compile time,
+// so one instance is small enough to stay resident in the instruction cache
+// when it is reused for several transforms (inverse transforms use
+// conj(fwd(conj(.)))).
+// ---------------------------------------------------------------------------
+template <int N, int Ns, typename C>
+__device__ __forceinline__ void fwd_passes_const(C* buf, int g, const C* __restrict__ tw, int off, C (&x)[16]) {
+  constexpr int G = N / 16;
+  constexpr int R = (N / Ns) >= 16 ? 16 : N / Ns;
+  if constexpr (Ns * R == N) {
+    last_pass_regs<R, 16, -1>(buf, g, G, N, Ns, tw + off, x);
+  } else {
+    stockham_pass<R, 16, -1>(buf, g, G, N, Ns, tw + off);
+    fwd_passes_const<N, Ns * R>(buf, g, tw, off + R * Ns, x);
+  }
+}
+
+template <int N, typename C>
+__device__ __forceinline__ void fwd_line_regs(C* buf, int g, const C* __restrict__ tw, C (&x)[16]) {
+  dft16<-1>(x);
+  if constexpr (N > 16) {
+    __syncwarp();  // earlier readers of buf are done
+#pragma unroll
+    for (int r = 0; r < 16; ++r) buf[padp(g * 16 + r)] = x[r];
+    __syncwarp();
+    fwd_passes_const<N, 16>(buf, g, tw, 16, x);
+  }
+}
+
 // Ampere-style asynchronous global->shared copies (LDGSTS); the data does not
 // pass through registers, so a whole tile can be in flight per thread block.
 __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {

@@ -289,6 +289,131 @@ __global__ void __launch_bounds__(64) k_zline_ns(ZArgs a) {
   }
 }
 
+__host__ __device__ inline size_t znsr_per_warp(int LD, int Kzp, int LPW) {
+  const size_t n = (size_t)LPW * ((size_t)6 * Kzp + (size_t)LD);
+  return (n + 1) & ~(size_t)1;
+}
+
+// Same sweep with the line length fixed at compile time and a single
+// forward-transform body reused for all five transforms of a line (the
+// three inverse ones as conj(fwd(conj(x))), the pack folded into the first
+// radix pass, the unpack done with warp shuffles).
+template <typename Real, int N>
+__global__ void __launch_bounds__(64, 6) k_zline_ns_t(ZArgs a) {
+  constexpr int E = 16, G = N / E, LPW = 32 / G;
+  using C = typename cplx_of<Real>::type;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const int LD = line_ld(N);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / G, g = lane % G;
+  const int Kzp = a.Kzp, Kz = a.Kz;
+  C* base = sm + (size_t)warp * znsr_per_warp(LD, Kzp, LPW);
+  C* stg = base + (size_t)sub * 6 * Kzp;
+  C* buf = base + (size_t)LPW * 6 * Kzp + (size_t)sub * LD;
+  const C* tw = reinterpret_cast<const C*>(a.tw);
+  const long long fs = a.nlines * Kzp;
+  const C* in = reinterpret_cast<const C*>(a.in);
+  C* out = reinterpret_cast<C*>(a.out);
+  const long long wstride = (long long)gridDim.x * (blockDim.x >> 5) * LPW;
+  const long long wfirst = ((long long)blockIdx.x * (blockDim.x >> 5) + warp) * LPW;
+  long long line = wfirst + sub;
+  constexpr int VB = 16 / (int)sizeof(C);
+  auto stage = [&](long long ln) {
+    if (ln < a.nlines) {
+      const int nchunk = 6 * Kzp / VB;
+      for (int q = g; q < nchunk; q += G) {
+        const int f = (q * VB) / Kzp, k = q * VB - f * Kzp;
+        cp_async16(stg + f * Kzp + k, in + f * fs + ln * Kzp + k);
+      }
+    }
+    cp_commit();
+  };
+  stage(line);
+  double rmax = 0.0;
+  const int src_lane = sub * G + ((G - g) & (G - 1));
+  for (long long wl = wfirst; wl < a.nlines; wl += wstride, line += wstride) {
+    const bool valid = line < a.nlines;
+    cp_wait_all();
+    __syncwarp();
+    C U0[E], U1[E], U2[E], X[E];
+#pragma unroll 1
+    for (int p = 0; p < 3; ++p) {
+      const C* ra = stg + (2 * p) * Kzp;
+      const C* rb = stg + (2 * p + 1) * Kzp;
+#pragma unroll
+      for (int m = 0; m < E; ++m) {
+        const int P = g + G * m;
+        C v = czero<C>();
+        if (valid) {
+          if (P < Kz) {
+            C A = ra[P], B = rb[P];
+            if (P == 0) { A.y = 0; B.y = 0; }
+            v = mk<C>(A.x - B.y, A.y + B.x);
+          } else if (N - P < Kz) {
+            const C A = ra[N - P], B = rb[N - P];
+            v = mk<C>(A.x + B.y, B.x - A.y);
+          }
+        }
+        X[m] = cconj(v);  // inverse = conj(fwd(conj(.)))
+      }
+      fwd_line_regs<N>(buf, g, tw, X);
+      if (p == 0) {
+#pragma unroll
+        for (int m = 0; m < E; ++m) U0[m] = cconj(X[m]);
+      } else if (p == 1) {
+#pragma unroll
+        for (int m = 0; m < E; ++m) U1[m] = cconj(X[m]);
+      } else {
+#pragma unroll
+        for (int m = 0; m < E; ++m) U2[m] = cconj(X[m]);
+      }
+    }
+    __syncwarp();
+    stage(line + wstride);
+    // u x w in registers; U0 = (ux, uy), U1 = (uz, wx), U2 = (wy, wz)
+    C Z[E];
+#pragma unroll
+    for (int m = 0; m < E; ++m) {
+      const Real u0 = U0[m].x, u1 = U0[m].y, u2 = U1[m].x, w0 = U1[m].y, w1 = U2[m].x, w2 = U2[m].y;
+      if (a.cfl_rate && valid)
+        rmax = fmax(rmax, fabs((double)u0) * a.inv_dx[0] + fabs((double)u1) * a.inv_dx[1] +
+                              fabs((double)u2) * a.inv_dx[2]);
+      X[m] = mk<C>(u1 * w2 - u2 * w1, u2 * w0 - u0 * w2);
+      Z[m] = mk<C>(u0 * w1 - u1 * w0, (Real)0);
+    }
+    fwd_line_regs<N>(buf, g, tw, X);
+    fwd_line_regs<N>(buf, g, tw, Z);
+    const long long lo = line * Kzp;
+#pragma unroll
+    for (int m = 0; m < E; ++m) {
+      const C snd = (g == 0) ? X[(E - m) & (E - 1)] : X[E - 1 - m];
+      C mir;
+      mir.x = __shfl_sync(0xffffffffu, snd.x, src_lane);
+      mir.y = __shfl_sync(0xffffffffu, snd.y, src_lane);
+      const int kz = g + G * m;
+      if (valid && kz < Kzp) {
+        C oa = czero<C>(), ob = czero<C>(), oc = czero<C>();
+        if (kz < Kz) {
+          const C Xm = X[m];
+          oa = mk<C>((Real)0.5 * (Xm.x + mir.x), (Real)0.5 * (Xm.y - mir.y));
+          ob = mk<C>((Real)0.5 * (Xm.y + mir.y), (Real)0.5 * (mir.x - Xm.x));
+          oc = Z[m];
+        }
+        out[lo + kz] = oa;
+        out[fs + lo + kz] = ob;
+        out[2 * fs + lo + kz] = oc;
+      }
+    }
+  }
+  cp_wait_all();
+  if (a.cfl_rate) {
+    for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    if (lane == 0 && rmax > 0.0)
+      atomicMax(reinterpret_cast<unsigned long long*>(a.cfl_rate), (unsigned long long)__double_as_longlong(rmax));
+  }
+}
+
 // C2R-only (MODE 1) and R2C-only (MODE 2) z sweeps of the unpruned
 // diagnostic transforms (not on the RK4 path).
 template <typename Real, int E, int MODE>
@@ -614,9 +739,37 @@ static int launch_z(const ZArgs& a, cudaStream_t s) {
   return (int)cudaGetLastError();
 }
 
+template <typename Real, int N>
+static int launch_zns_t(const ZArgs& a, cudaStream_t s) {
+  using C = typename cplx_of<Real>::type;
+  constexpr int G = N / 16, LPW = 32 / G;
+  const int warps = 2;
+  if (a.Kzp % 8 != 0 || a.n != N) return (int)cudaErrorInvalidValue;
+  const size_t sm = (size_t)warps * znsr_per_warp(line_ld(N), a.Kzp, LPW) * sizeof(C);
+  auto kern = k_zline_ns_t<Real, N>;
+  int dev = 0, nsm = 148, occ = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, warps * 32, sm);
+  if (occ < 1) occ = 1;
+  const long long per_block = (long long)warps * LPW;
+  long long nb = (a.nlines + per_block - 1) / per_block;
+  if (nb > (long long)occ * nsm) nb = (long long)occ * nsm;
+  kern<<<(unsigned)nb, warps * 32, sm, s>>>(a);
+  return (int)cudaGetLastError();
+}
+
 template <typename Real>
 int Kernels<Real>::zline_ns(const ZArgs& a, cudaStream_t s) {
-  return elems_for(a.n) == 16 ? launch_zns<Real, 16>(a, s) : launch_zns<Real, 32>(a, s);
+  switch (a.n) {
+    case 16: return launch_zns_t<Real, 16>(a, s);
+    case 32: return launch_zns_t<Real, 32>(a, s);
+    case 64: return launch_zns_t<Real, 64>(a, s);
+    case 128: return launch_zns_t<Real, 128>(a, s);
+    case 256: return launch_zns_t<Real, 256>(a, s);
+    case 512: return launch_zns_t<Real, 512>(a, s);
+    default: return launch_zns<Real, 32>(a, s);
+  }
 }
 template <typename Real>
 int Kernels<Real>::zline_c2r(const ZArgs& a, cudaStream_t s) {
@@ -670,6 +823,8 @@ int Kernels<Real>::smem_optin(int dev) {
   SDNS_OPT((k_axis<Real, 16, -1, 0>)); SDNS_OPT((k_axis<Real, 16, 1, 0>)); SDNS_OPT((k_axis<Real, 16, 1, 1>));
   SDNS_OPT((k_axis<Real, 32, -1, 0>)); SDNS_OPT((k_axis<Real, 32, 1, 0>)); SDNS_OPT((k_axis<Real, 32, 1, 1>));
   SDNS_OPT((k_zline_ns<Real, 16>)); SDNS_OPT((k_zline_ns<Real, 32>));
+  SDNS_OPT((k_zline_ns_t<Real, 16>)); SDNS_OPT((k_zline_ns_t<Real, 32>)); SDNS_OPT((k_zline_ns_t<Real, 64>));
+  SDNS_OPT((k_zline_ns_t<Real, 128>)); SDNS_OPT((k_zline_ns_t<Real, 256>)); SDNS_OPT((k_zline_ns_t<Real, 512>));
   SDNS_OPT((k_zline<Real, 16, 1>)); SDNS_OPT((k_zline<Real, 16, 2>));
   SDNS_OPT((k_zline<Real, 32, 1>)); SDNS_OPT((k_zline<Real, 32, 2>));
   SDNS_OPT((k_axis_rk<Real, 16>)); SDNS_OPT((k_axis_rk<Real, 32>));

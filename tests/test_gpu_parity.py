@@ -40,7 +40,8 @@ def test_transforms(built_lib, N, L, prec):
 
 
 @pytest.mark.parametrize("prec", ["double", "single"])
-@pytest.mark.parametrize("N,L", GRIDS)
+@pytest.mark.parametrize("N,L", GRIDS + [((16, 16, 512), (2 * np.pi,) * 3), ((16, 32, 256), (2 * np.pi,) * 3),
+                                          ((128, 16, 128), (2 * np.pi,) * 3)])
 def test_compute_rhs(built_lib, N, L, prec):
     g = Grid(N, L)
     uh = random_state(g, seed=3)
