@@ -1,0 +1,84 @@
+"""The oracle against the reference's own known answers and fixtures (CPU only)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from oracle.ns_ref import Grid, dealias_cutoff, run_tg, taylor_green
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden", "short64.npz")
+sys.path.insert(0, os.path.join(HERE, "golden"))
+
+
+@pytest.mark.parametrize("N,L", [((16, 16, 16), (2 * np.pi,) * 3), ((32, 32, 32), (2 * np.pi,) * 3),
+                                 ((64, 32, 16), (6 * np.pi, 4 * np.pi, 2 * np.pi))])
+def test_tg_known_answers(N, L):
+    """tests/TG.py:125-126 (7 digits, ntol default config.py:196)."""
+    k, w, _ = run_tg(N, L=L)
+    assert round(k - 0.124953117517, 7) == 0
+    assert round(w - 0.375249930801, 7) == 0
+
+
+def test_short_script_tg_state():
+    """State after 10 RK4 steps equals the reference's spectralDNS3D_short.py (N=64)."""
+    d = np.load(GOLD)
+    N = int(d["N"])
+    S = float(N ** 3)  # the short script's forward transform is unnormalised
+    _, _, uh = run_tg((N, N, N))
+    idx = tuple(d["tg_idx"].astype(int).T)
+    assert np.max(np.abs(uh[idx] * S - d["tg_val"])) / np.max(np.abs(d["tg_val"])) < 1e-14
+    mask = np.ones(uh.shape, bool)
+    mask[idx] = False
+    assert np.abs(uh[mask]).max() * S < 1e-9
+    assert abs(float(d["tg_k"]) - 0.124953117517) < 5e-13
+
+
+def test_short_script_compute_rhs():
+    """ComputeRHS on a seeded random field equals the short script's (N=64)."""
+    from make_golden import random_input
+    d = np.load(GOLD)
+    N = int(d["N"])
+    S = float(N ** 3)
+    g = Grid((N, N, N))
+    rhs = g.compute_rhs(random_input(int(d["rhs_seed"]), N) / S) * S
+    idx = tuple(d["rhs_idx"].astype(int).T)
+    assert np.max(np.abs(rhs[idx] - d["rhs_val"])) / np.max(np.abs(d["rhs_val"])) < 1e-13
+
+
+def test_dealias_cutoffs():
+    # |k| < 2/3 (N/2+1)
+    assert [dealias_cutoff(n) for n in (16, 32, 64, 128, 256, 512, 1024)] == [5, 11, 21, 43, 85, 171, 341]
+    assert dealias_cutoff(32, "None") == 15
+
+
+def test_parseval_and_divergence_free():
+    g = Grid((32, 32, 32))
+    uh = g.forward(taylor_green(g))
+    assert abs(0.5 * g.energy_fourier(uh) - g.kinetic_energy(uh)) < 1e-14
+    assert g.divergence_ms(uh) < 1e-28
+    rhs = g.compute_rhs(uh)
+    assert np.max(np.abs(sum(g.K[i] * (rhs[i] + g.nu * g.K2 * uh[i]) for i in range(3)))) < 1e-12
+
+
+def test_forcing_injects_eps():
+    from spectraldns_gb300.init import isotropic_field
+    g = Grid((32, 32, 32), nu=0.0)
+    uh = isotropic_field((32, 32, 32), k0=2.0, seed=3, dtype=np.complex128)
+    src = g.forcing_source(uh, 0.1, 2.0)
+    w = g.hermitian_weights()
+    power = float(np.sum((np.conj(uh) * src).real * w))
+    assert abs(power - 0.1) < 1e-12
+
+
+def test_isotropic_field_properties():
+    from spectraldns_gb300.init import isotropic_field
+    g = Grid((64, 64, 64))
+    uh = isotropic_field((64, 64, 64), k0=4.0, energy=0.5, seed=0, dtype=np.complex128)
+    assert abs(0.5 * g.energy_fourier(uh) - 0.5) < 1e-6
+    assert g.divergence_ms(uh) < 1e-12
+    assert np.abs(uh * (~g.mask)).max() == 0
+    assert np.abs(g.forward(g.backward(uh)) - uh).max() < 1e-12  # spectrum of a real field
+    E = g.shell_spectrum(uh)
+    assert 3 <= int(np.argmax(E)) <= 5  # k^4 exp(-2 (k/4)^2) peaks at k = 4
