@@ -129,6 +129,24 @@ int sdns_spectrum(sdns_ctx* ctx, double* Ek, int32_t nbins);
 int sdns_set_timing(sdns_ctx* ctx, int32_t on);
 int sdns_get_timing(sdns_ctx* ctx, double* ms /* 8 */, int32_t* launches /* 8 */);
 
+/* ComputeRHS that allocates nothing.  This entry point has no counterpart in
+ * the reference.  It serves callers that must not call cudaMalloc: work
+ * recorded into a CUDA graph, programs whose framework allocator owns the
+ * device memory, real-time loops.  It takes the grid description instead of
+ * a context, the caller's device arrays u_hat and rhs (spectral vector
+ * layout, complex64 or complex128 per cfg->precision, on device cfg->device)
+ * and a cudaStream_t (NULL: the legacy default stream), and enqueues the
+ * same computation as sdns_compute_rhs with the Source term zero.  Its
+ * scratch is one static device array of SDNS_NOALLOC_SCRATCH_BYTES that every
+ * GPU loading the library keeps until the process exits; grids that need
+ * more (about 64^3 in double, 64x64x128 in single precision is the limit)
+ * are rejected with SDNS_EINVAL.  The first call on a device looks up the
+ * array's device address, so make that call before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller.  Errors are reported through sdns_last_error. */
+#define SDNS_NOALLOC_SCRATCH_BYTES (32 * 1024 * 1024)
+int sdns_compute_rhs_noalloc(const sdns_config* cfg, const void* u_hat, void* rhs, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -66,6 +66,7 @@ SIGNATURES = {
     "sdns_spectrum": (C.c_int, [_CTX, C.POINTER(C.c_double), C.c_int32]),
     "sdns_set_timing": (C.c_int, [_CTX, C.c_int32]),
     "sdns_get_timing": (C.c_int, [_CTX, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
+    "sdns_compute_rhs_noalloc": (C.c_int, [C.POINTER(sdns_config), _P, _P, _P]),
 }
 
 _lib = None

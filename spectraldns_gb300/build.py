@@ -24,6 +24,7 @@ SOURCES = [
     "sdns_kernels_f32.cu",
     "sdns_kernels_f64.cu",
     "sdns_capi.cu",
+    "sdns_noalloc.cu",
 ]
 EXTRA_SOURCES: list = []  # appended by later modules (LES closure kernels)
 

@@ -64,6 +64,8 @@ enum { SC_DT = 0, SC_RATE = 1, SC_ALPHA = 2, SC_TIME = 3, SC_LASTRATE = 4, SC_EN
 
 }  // namespace
 
+void sdns::set_last_error(const char* msg) { g_err = msg ? msg : ""; }
+
 struct sdns_ctx {
   sdns_config cfg;
   int dev = 0;

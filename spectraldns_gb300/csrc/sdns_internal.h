@@ -104,6 +104,9 @@ struct RKArgs {
   double* partials;          // [gridDim.x][4] energy, enstrophy sums (stage 3)
 };
 
+// message returned by sdns_last_error() (thread-local)
+void set_last_error(const char* msg);
+
 template <typename Real> struct Kernels {
   static int axis_plain(const AxisArgs& a, int sign, cudaStream_t s);
   static int axis_curl_inv(const AxisArgs& a, cudaStream_t s);
