@@ -115,11 +115,13 @@ int sdns_set_time(sdns_ctx* ctx, double t);
 /* transforms of nfields (1..3) scalar fields stacked on the first axis */
 int sdns_forward(sdns_ctx* ctx, const void* phys, void* spec, int32_t nfields, int where);
 int sdns_backward(sdns_ctx* ctx, const void* spec, void* phys, int32_t nfields, int where);
-/* physical fields computed from the context state */
+/* physical fields: velocity of the context state; curl and divergence of the
+ * spectral vector u_hat (NULL: of the context state); pressure of the last
+ * right-hand-side evaluation (needs store_pressure) */
 int sdns_velocity(sdns_ctx* ctx, void* u, int where);
-int sdns_curl(sdns_ctx* ctx, void* curl, int where);
+int sdns_curl(sdns_ctx* ctx, const void* u_hat, void* curl, int where);
 int sdns_pressure(sdns_ctx* ctx, void* p, int where);
-int sdns_divergence(sdns_ctx* ctx, void* div, int where);
+int sdns_divergence(sdns_ctx* ctx, const void* u_hat, void* div, int where);
 
 int sdns_diagnostics(sdns_ctx* ctx, double* out /* SDNS_DIAG_COUNT */);
 int sdns_spectrum(sdns_ctx* ctx, double* Ek, int32_t nbins);

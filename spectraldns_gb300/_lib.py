@@ -59,9 +59,9 @@ SIGNATURES = {
     "sdns_forward": (C.c_int, [_CTX, _P, _P, C.c_int32, C.c_int]),
     "sdns_backward": (C.c_int, [_CTX, _P, _P, C.c_int32, C.c_int]),
     "sdns_velocity": (C.c_int, [_CTX, _P, C.c_int]),
-    "sdns_curl": (C.c_int, [_CTX, _P, C.c_int]),
+    "sdns_curl": (C.c_int, [_CTX, _P, _P, C.c_int]),
     "sdns_pressure": (C.c_int, [_CTX, _P, C.c_int]),
-    "sdns_divergence": (C.c_int, [_CTX, _P, C.c_int]),
+    "sdns_divergence": (C.c_int, [_CTX, _P, _P, C.c_int]),
     "sdns_diagnostics": (C.c_int, [_CTX, C.POINTER(C.c_double)]),
     "sdns_spectrum": (C.c_int, [_CTX, C.POINTER(C.c_double), C.c_int32]),
     "sdns_set_timing": (C.c_int, [_CTX, C.c_int32]),

@@ -1079,12 +1079,23 @@ int sdns_velocity(sdns_ctx* c, void* u, int where) {
   return copy_out(c, u, c->PH, 3 * c->nphys1 * (long long)c->rsz, where);
 }
 
-int sdns_curl(sdns_ctx* c, void* w, int where) {
+// spectral vector (caller layout) or, when u_hat is NULL, the context state -> padded F2
+int spectral_to_padded(sdns_ctx* c, const void* u_hat, int where) {
+  int e;
+  if (!u_hat) {
+    if (!c->has_state) return fail(SDNS_ESTATE, "no state set");
+    return state_to_padded(c, c->F2);
+  }
+  if ((e = ensure_stage(c))) return e;
+  if ((e = copy_in(c, c->stage, u_hat, 3 * c->nfull1 * (long long)c->csz, where))) return e;
+  return repitch(c, c->stage, c->F2, 3, c->N2h, c->Kzpf, c->N2h);
+}
+
+int sdns_curl(sdns_ctx* c, const void* u_hat, void* w, int where) {
   int e = check_ctx(c);
   if (e) return e;
-  if (!c->has_state) return fail(SDNS_ESTATE, "no state set");
   if ((e = ensure_full_bufs(c))) return e;
-  if ((e = state_to_padded(c, c->F2))) return e;
+  if ((e = spectral_to_padded(c, u_hat, where))) return e;
   Geo g = geo(c);
   if (c->dbl) k_curl_div<double2><<<nblocks(c->npadf1), 256, 0, c->st>>>((const double2*)c->F2, (double2*)c->F1, g, 0);
   else k_curl_div<float2><<<nblocks(c->npadf1), 256, 0, c->st>>>((const float2*)c->F2, (float2*)c->F1, g, 0);
@@ -1093,12 +1104,11 @@ int sdns_curl(sdns_ctx* c, void* w, int where) {
   return copy_out(c, w, c->PH, 3 * c->nphys1 * (long long)c->rsz, where);
 }
 
-int sdns_divergence(sdns_ctx* c, void* d, int where) {
+int sdns_divergence(sdns_ctx* c, const void* u_hat, void* d, int where) {
   int e = check_ctx(c);
   if (e) return e;
-  if (!c->has_state) return fail(SDNS_ESTATE, "no state set");
   if ((e = ensure_full_bufs(c))) return e;
-  if ((e = state_to_padded(c, c->F2))) return e;
+  if ((e = spectral_to_padded(c, u_hat, where))) return e;
   Geo g = geo(c);
   if (c->dbl) k_curl_div<double2><<<nblocks(c->npadf1), 256, 0, c->st>>>((const double2*)c->F2, (double2*)c->F1, g, 1);
   else k_curl_div<float2><<<nblocks(c->npadf1), 256, 0, c->st>>>((const float2*)c->F2, (float2*)c->F1, g, 1);

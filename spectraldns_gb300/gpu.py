@@ -209,14 +209,32 @@ class Context:
     def velocity(self, out=None):
         return self._phys(self._L.sdns_velocity, out, 3)
 
-    def curl(self, out=None):
-        return self._phys(self._L.sdns_curl, out, 3)
+    def _phys_of(self, fn, u_hat, out, nf):
+        """fn(ctx, u_hat or NULL, out, where) for the spectral vector u_hat (None: the state)."""
+        shape = self.phys_shape if nf == 3 else self.phys_shape[1:]
+        if u_hat is None:
+            p, w, arr, wb = self._arg_out(out, self.real, shape)
+            check(fn(self._h, None, C.c_void_p(p), w))
+            return self._finish(arr, wb, w)
+        q, w1, keep = self._arg_in(u_hat, self.complex, self.spec_shape)
+        if w1 == _lib.SDNS_DEVICE and out is None:
+            out = torch.empty(shape, dtype=_torch_dtype(self.real), device=keep.device)
+        p, w, arr, wb = self._arg_out(out, self.real, shape)
+        if w != w1:
+            raise ValueError("input and output must both be host or both be device arrays")
+        check(fn(self._h, C.c_void_p(q), C.c_void_p(p), w))
+        return self._finish(arr, wb, w)
+
+    def curl(self, u_hat=None, out=None):
+        """F^-1(i K x u_hat); u_hat None: of the context state."""
+        return self._phys_of(self._L.sdns_curl, u_hat, out, 3)
 
     def pressure(self, out=None):
         return self._phys(self._L.sdns_pressure, out, 1)
 
-    def divergence(self, out=None):
-        return self._phys(self._L.sdns_divergence, out, 1)
+    def divergence(self, u_hat=None, out=None):
+        """F^-1(i K . u_hat); u_hat None: of the context state."""
+        return self._phys_of(self._L.sdns_divergence, u_hat, out, 1)
 
     def diagnostics(self):
         buf = (C.c_double * _lib.SDNS_DIAG_COUNT)()

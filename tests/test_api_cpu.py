@@ -1,0 +1,91 @@
+"""Host-side logic of the spectralDNS-compatible API (no GPU needed)."""
+import os
+import runpy
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = "/root/reference"
+
+
+def test_params_semantics():
+    from spectraldns_gb300 import config
+    p = config.Params()
+    p.precision = "single"
+    p.nu = 0.000625
+    p.dt = 0.01
+    assert isinstance(p.nu, np.float32) and isinstance(p.dt, np.float32)
+    p.precision = "double"
+    assert isinstance(p.nu, np.float64)
+    p.M = [5, 4, 3]
+    assert list(p.N) == [32, 16, 8]
+    p.L = ["2*pi", "4*pi", 1.5]
+    assert np.allclose(p.L, [2 * np.pi, 4 * np.pi, 1.5])
+    assert np.allclose(p.dx, p.L / p.N)
+    with pytest.raises(ValueError):
+        p.L = ["__import__('os')", 1, 1]
+
+
+def test_get_solver_parses_flags():
+    from spectraldns_gb300 import config, get_solver
+    config.update({"nu": 0.001, "dt": 0.005, "T": 0.02}, "triplyperiodic")
+    sol = get_solver(parse_args=["--M", "4", "5", "4", "--precision", "single", "NS"])
+    assert sol.__name__.endswith("solvers.NS")
+    assert list(config.params.N) == [16, 32, 16]
+    assert config.params.precision == "single" and abs(float(config.params.dt) - 0.005) < 1e-9
+    assert config.solver is sol
+    with pytest.raises(SystemExit):
+        get_solver(parse_args=["MHD"])  # not a solver of this backend
+
+
+def test_end_of_tstep_snaps_to_T():
+    from spectraldns_gb300 import config, get_solver
+    sol = get_solver(parse_args=["NS"])
+    config.params.T = 0.1
+    config.params.t = 0.095
+    config.params.dt = 0.01
+    assert not sol.end_of_tstep(None)
+    assert abs(float(config.params.dt) - 0.005) < 1e-12
+
+
+def test_checkpoint_and_kill_file(tmp_path, monkeypatch):
+    from spectraldns_gb300 import config
+    from spectraldns_gb300.solvers.NS import NSFile
+    monkeypatch.chdir(tmp_path)
+    p = config.Params(t=0.5, tstep=4, checkpoint=2, write_result=100)
+    U_hat = np.ones((3, 4, 4, 3), complex)
+    f = NSFile(str(tmp_path / "run"))
+    f.update(p, U_hat=U_hat)
+    d = np.load(str(tmp_path / "run_c.npz"))
+    assert d["tstep"] == 4 and np.allclose(d["U_hat"], 1)
+    open("killspectraldns", "w").close()
+    p.tstep = 5
+    with pytest.raises(SystemExit):
+        f.update(p, U_hat=2 * U_hat)
+    assert np.allclose(np.load(str(tmp_path / "run_c.npz"))["U_hat"], 2)
+
+
+def test_energy_fourier_shim():
+    sys.path.insert(0, os.path.join(ROOT, "spectraldns_gb300", "compat"))
+    try:
+        from shenfun.fourier import energy_fourier
+        from oracle.ns_ref import Grid, taylor_green
+        g = Grid((16, 16, 16))
+        uh = g.forward(taylor_green(g))
+        assert abs(energy_fourier(uh) - g.energy_fourier(uh)) < 1e-15
+    finally:
+        sys.path.pop(0)
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
+@pytest.mark.parametrize("demo", ["TG.py", "Isotropic.py"])
+def test_reference_demos_import_through_shims(demo):
+    code = ("import runpy, warnings; warnings.simplefilter('ignore'); "
+            "ns = runpy.run_path(%r, run_name='demo'); print(sorted(k for k in ns if not k.startswith('_'))[:3])"
+            % os.path.join(REF, "demo", demo))
+    import subprocess
+    env = dict(os.environ, PYTHONPATH=os.pathsep.join([os.path.join(ROOT, "spectraldns_gb300", "compat"), ROOT]))
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
