@@ -131,6 +131,45 @@ int sdns_spectrum(sdns_ctx* ctx, double* Ek, int32_t nbins);
 int sdns_set_timing(sdns_ctx* ctx, int32_t on);
 int sdns_get_timing(sdns_ctx* ctx, double* ms /* 8 */, int32_t* launches /* 8 */);
 
+/* ---- learned subgrid-stress closure for a coarse LES (no counterpart in the
+ * reference; the benchmark's LES case).  Device pointers, caller stream. ---- */
+/* box filter of ratio r: fine velocity (3, N0, N1, N2) real -> coarse
+ * ubar (3, n0, n1, n2) float and tau (n0*n1*n2, 6) float, tau_ij =
+ * bar(u_i u_j) - bar(u_i) bar(u_j) in the order xx yy zz xy xz yz */
+int sdns_les_box_filter(const void* u, int32_t precision, const int32_t* N, int32_t ratio, float* ubar, float* tau,
+                        void* stream);
+/* ghat[3 i + j] = i K_j uhat_i for a spectral vector (3, n0, n1, n2/2+1) */
+int sdns_les_grad_hat(const void* uhat, void* ghat, int32_t precision, const int32_t* n, const double* L,
+                      void* stream);
+/* SGS force -P(i K_j tauhat_ij) * scale from tauhat (6, n0, n1, n2/2+1) */
+int sdns_les_sgs_force(const void* tauhat, void* force, int32_t precision, const int32_t* n, const double* L,
+                       double scale, void* stream);
+/* planar float (nch, P) <-> channels-last (P, cpad): pack -> bf16 with (x - mu) * isd,
+ * unpack float -> planar with y * sd + mu */
+int sdns_les_pack(const float* x, int32_t nch, int64_t P, int32_t cpad, const float* mu, const float* isd, void* y,
+                  void* stream);
+int sdns_les_unpack(const float* y, int32_t cpad, int32_t nch, int64_t P, const float* mu, const float* sd, float* x,
+                    void* stream);
+/* periodic 3x3x3 convolution, channels last, bf16 activations and weights
+ * W (27, co, ci), FP32 accumulation; (ci, co) in {(16,32), (32,32), (32,8)};
+ * forward writes the FP32 pre-activation y and (optional) the bf16
+ * activation yact (ReLU when relu != 0); grid sides multiples of 8 */
+int sdns_conv3d_fwd(const void* x, const void* W, const float* b, float* y, void* yact, const int32_t* n, int32_t ci,
+                    int32_t co, int32_t relu, void* stream);
+int sdns_conv3d_bwd_data(const float* gpre, const void* W, float* gin, const int32_t* n, int32_t ci, int32_t co,
+                         void* stream);
+/* accumulates (+=) into dW (27, co, ci) and db (co) */
+int sdns_conv3d_bwd_weight(const void* x, const float* gpre, float* dW, float* db, const int32_t* n, int32_t ci,
+                           int32_t co, void* stream);
+int sdns_relu_bwd(const float* gpost, const float* pre, float* gpre, int64_t count, int32_t relu, void* stream);
+/* grad = 2 (y - t) / (P nch) over the first nch of cpad channels; *loss += mean square */
+int sdns_mse_grad(const float* y, int32_t cpad, int32_t nch, const float* target, int64_t P, float* grad, double* loss,
+                  void* stream);
+/* Adam step (step >= 1) on FP32 weights; refreshes the bf16 copy when wbf16 != NULL */
+int sdns_adam_step(float* w, const float* g, float* m, float* v, int64_t count, float lr, float b1, float b2,
+                   float eps, int32_t step, void* wbf16, void* stream);
+int sdns_to_bf16(const float* a, void* b, int64_t count, void* stream);
+
 /* ComputeRHS that allocates nothing.  This entry point has no counterpart in
  * the reference.  It serves callers that must not call cudaMalloc: work
  * recorded into a CUDA graph, programs whose framework allocator owns the

@@ -67,6 +67,20 @@ SIGNATURES = {
     "sdns_set_timing": (C.c_int, [_CTX, C.c_int32]),
     "sdns_get_timing": (C.c_int, [_CTX, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "sdns_compute_rhs_noalloc": (C.c_int, [C.POINTER(sdns_config), _P, _P, _P]),
+    # learned-closure LES
+    "sdns_les_box_filter": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P]),
+    "sdns_les_grad_hat": (C.c_int, [_P, _P, C.c_int32, _P, _P, _P]),
+    "sdns_les_sgs_force": (C.c_int, [_P, _P, C.c_int32, _P, _P, C.c_double, _P]),
+    "sdns_les_pack": (C.c_int, [_P, C.c_int32, C.c_int64, C.c_int32, _P, _P, _P, _P]),
+    "sdns_les_unpack": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int64, _P, _P, _P, _P]),
+    "sdns_conv3d_fwd": (C.c_int, [_P, _P, _P, _P, _P, _P, C.c_int32, C.c_int32, C.c_int32, _P]),
+    "sdns_conv3d_bwd_data": (C.c_int, [_P, _P, _P, _P, C.c_int32, C.c_int32, _P]),
+    "sdns_conv3d_bwd_weight": (C.c_int, [_P, _P, _P, _P, _P, C.c_int32, C.c_int32, _P]),
+    "sdns_relu_bwd": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int32, _P]),
+    "sdns_mse_grad": (C.c_int, [_P, C.c_int32, C.c_int32, _P, C.c_int64, _P, _P, _P]),
+    "sdns_adam_step": (C.c_int, [_P, _P, _P, _P, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32,
+                                 _P, _P]),
+    "sdns_to_bf16": (C.c_int, [_P, _P, C.c_int64, _P]),
 }
 
 _lib = None

@@ -25,6 +25,7 @@ SOURCES = [
     "sdns_kernels_f64.cu",
     "sdns_capi.cu",
     "sdns_noalloc.cu",
+    "sdns_les.cu",
 ]
 EXTRA_SOURCES: list = []  # appended by later modules (LES closure kernels)
 

@@ -920,7 +920,8 @@ int sdns_get_state(sdns_ctx* c, void* u_hat, int where) {
 int sdns_set_source(sdns_ctx* c, const void* source, int where) {
   int e = check_ctx(c);
   if (e) return e;
-  c->gkey = ~0ull;
+  // the RK4 graph depends on whether a source exists, not on its values
+  if (!source || !c->src) c->gkey = ~0ull;
   if (!source) {
     if (c->src) { cudaFree(c->src); c->bytes -= 3 * c->ncomp1 * 16; c->src = nullptr; }
     if (c->src_full) { cudaFree(c->src_full); c->bytes -= 3 * c->nfull1 * c->csz; c->src_full = nullptr; }
