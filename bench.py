@@ -50,7 +50,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--les", action="store_true", help="also time the closure LES (if built)")
+    p.add_argument("--no-les", action="store_true", help="skip the closure-LES timing")
     return p.parse_args()
 
 
@@ -168,6 +168,7 @@ def run_ours(args):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     ctx.set_timing(True)
+    t_start = ctx.diagnostics()["time"]
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
@@ -183,6 +184,7 @@ def run_ours(args):
     ktimes, klaunch = ctx.get_timing()
     ctx.set_timing(False)
     diag = ctx.diagnostics()
+    dns_s_per_sim_time = (ms / 1e3) / max(diag["time"] - t_start, 1e-30)
     t_ms = torch.tensor([ms], device="cuda:%d" % dev)
     if ws > 1:
         torch.distributed.all_reduce(t_ms, op=torch.distributed.ReduceOp.MAX)
@@ -275,12 +277,65 @@ def run_ours(args):
                        "ms_per_step": m64 / k64, "dtype": "f64"}
         c64.close()
 
+    if not args.no_les and n >= 64:
+        out["les"] = les_measure(dev, n, dns_s_per_sim_time)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_sample(512 if n >= 512 else n)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def les_measure(dev, n_dns, dns_s_per_sim_time, ratio=8, steps=30):
+    """GPU time per unit simulated time of the 64^3 closure LES (network inference + RK4 step),
+    timed on this GPU, against the DNS measured above; spectrum errors from the committed
+    closure experiment (profiles/les_closure_512to64.json)."""
+    import torch
+    from spectraldns_gb300 import les as L
+    from spectraldns_gb300.init import isotropic_field
+    nc = n_dns // ratio
+    n = (nc,) * 3
+    model = os.path.join(ROOT, "spectraldns_gb300", "data", "closure_%d.npz" % nc)
+    if os.path.exists(model):
+        net, nm = L.load_model(model, n, device=dev)
+        trained = True
+    else:
+        net = L.ClosureNet(n, device=dev)
+        d = torch.device("cuda", dev)
+        nm = {"fmu": torch.zeros(9, device=d), "fisd": torch.ones(9, device=d), "tmu": torch.zeros(6, device=d),
+              "tsd": torch.full((6,), 1e-3, device=d)}
+        trained = False
+    les = L.LES(n, net, nm, device=dev)
+    les.ctx.set_state(isotropic_field(n, k0=4.0, energy=0.5, seed=0, dtype=np.complex64))
+    for _ in range(3):
+        les.step()
+    les.ctx.synchronize()
+    t0 = les.time()
+    w0 = time.perf_counter()
+    for _ in range(steps):
+        les.step()
+    les.ctx.synchronize()
+    wall = time.perf_counter() - w0
+    sim = les.time() - t0
+    les_s = wall / max(sim, 1e-30)
+    out = {"value": dns_s_per_sim_time / les_s, "unit": "x fewer GPU-seconds per simulated time than the %d^3 DNS"
+           % n_dns, "les_grid": list(n), "les_ms_per_step": 1e3 * wall / steps, "les_s_per_sim_time": les_s,
+           "dns_s_per_sim_time": dns_s_per_sim_time, "trained_weights": trained,
+           "timing": "wall clock around steps x (closure inference + RK4 step), synchronised"}
+    try:
+        with open(os.path.join(ROOT, "profiles", "les_closure_512to64.json")) as f:
+            ex = json.load(f)
+        ev = ex["evaluation"]
+        out["spectrum_err_k<=20"] = {"closure_final": ev["closure"]["max_err_k<=20_final"],
+                                     "closure_mean": ev["closure"]["max_err_k<=20_mean"],
+                                     "no_closure_final": ev["no_closure"]["max_err_k<=20_final"],
+                                     "no_closure_mean": ev["no_closure"]["max_err_k<=20_mean"],
+                                     "source": "profiles/les_closure_512to64.json"}
+    except Exception:
+        pass
+    les.ctx.close()
+    return out
 
 
 def cpu_stage(n, workers):

@@ -330,7 +330,8 @@ __global__ void __launch_bounds__(64, 6) k_zline_ns_t(ZArgs a) {
     cp_commit();
   };
   stage(line);
-  double rmax = 0.0;
+  Real rmax = 0;  // CFL rate in the working precision (FP32: no FP64 arithmetic per point)
+  const Real idx0 = (Real)a.inv_dx[0], idx1 = (Real)a.inv_dx[1], idx2 = (Real)a.inv_dx[2];
   const int src_lane = sub * G + ((G - g) & (G - 1));
   for (long long wl = wfirst; wl < a.nlines; wl += wstride, line += wstride) {
     const bool valid = line < a.nlines;
@@ -376,9 +377,7 @@ __global__ void __launch_bounds__(64, 6) k_zline_ns_t(ZArgs a) {
 #pragma unroll
     for (int m = 0; m < E; ++m) {
       const Real u0 = U0[m].x, u1 = U0[m].y, u2 = U1[m].x, w0 = U1[m].y, w1 = U2[m].x, w2 = U2[m].y;
-      if (a.cfl_rate && valid)
-        rmax = fmax(rmax, fabs((double)u0) * a.inv_dx[0] + fabs((double)u1) * a.inv_dx[1] +
-                              fabs((double)u2) * a.inv_dx[2]);
+      if (a.cfl_rate && valid) rmax = fmax(rmax, fabs(u0) * idx0 + fabs(u1) * idx1 + fabs(u2) * idx2);
       X[m] = mk<C>(u1 * w2 - u2 * w1, u2 * w0 - u0 * w2);
       Z[m] = mk<C>(u0 * w1 - u1 * w0, (Real)0);
     }
@@ -409,8 +408,9 @@ __global__ void __launch_bounds__(64, 6) k_zline_ns_t(ZArgs a) {
   cp_wait_all();
   if (a.cfl_rate) {
     for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
-    if (lane == 0 && rmax > 0.0)
-      atomicMax(reinterpret_cast<unsigned long long*>(a.cfl_rate), (unsigned long long)__double_as_longlong(rmax));
+    const double rm = (double)rmax;
+    if (lane == 0 && rm > 0.0)
+      atomicMax(reinterpret_cast<unsigned long long*>(a.cfl_rate), (unsigned long long)__double_as_longlong(rm));
   }
 }
 

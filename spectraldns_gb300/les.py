@@ -388,8 +388,21 @@ def run_experiment(out_json, n_dns=512, ratio=8, steps=2000, every=10, iters=150
            "speedup_no_closure": dns_s_per_time / ev["no_closure"]["s_per_sim_time"]}
     with open(out_json, "w") as f:
         json.dump(out, f, indent=1)
-    np.save(os.path.splitext(out_json)[0] + "_weights.npy", net.state_dict()["w"])
+    save_model(os.path.splitext(out_json)[0] + "_model.npz", net, nm)
     return out
+
+
+def save_model(path, net, nm):
+    np.savez(path, w=net.state_dict()["w"], **{k: v.cpu().numpy() for k, v in nm.items()})
+
+
+def load_model(path, n, device=0):
+    d = np.load(path)
+    net = ClosureNet(n, device=device)
+    net.load(d["w"])
+    dev = torch.device("cuda", device)
+    nm = {k: torch.from_numpy(d[k]).to(dev) for k in ("fmu", "fisd", "tmu", "tsd")}
+    return net, nm
 
 
 if __name__ == "__main__":

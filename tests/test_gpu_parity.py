@@ -131,3 +131,42 @@ def test_diagnostics_and_spectrum(built_lib):
     assert relerr(c.spectrum(len(Ek)), Ek) < 1e-12
     assert relerr(c.divergence(), g.backward(1j * sum(g.K[i] * uh[i] for i in range(3)))) < 1e-6 or \
         np.max(np.abs(c.divergence())) < 1e-12
+
+
+@pytest.mark.parametrize("prec", ["double", "single"])
+def test_forcing_and_cfl_step(built_lib, prec):
+    """One RK4 step with constant-power forcing (Source from the step-start state) and the CFL
+    time step dt = cfl / max(|u|/dx + |v|/dy + |w|/dz), against the oracle."""
+    from spectraldns_gb300.init import isotropic_field
+    N = (32, 32, 32)
+    g = Grid(N, nu=0.01)
+    uh = isotropic_field(N, k0=3.0, energy=0.5, seed=4, dtype=np.complex128)
+    c = ctx(N, (2 * np.pi,) * 3, prec, nu=0.01)
+    c.set_forcing(0.1, 2.0)
+    c.set_cfl(0.5)
+    c.set_state(uh.astype(c.complex))
+    c.rk4(0.0, 1)
+    rate = g.cfl_rate(uh)
+    dt = 0.5 / rate
+    ref = g.rk4_step(uh, dt, source=g.forcing_source(uh, 0.1, 2.0))
+    d = c.diagnostics()
+    tol = 1e-11 if prec == "double" else 2e-5
+    assert abs(d["cfl_rate"] - rate) / rate < (1e-13 if prec == "double" else 1e-6)
+    assert abs(d["last_dt"] - dt) / dt < (1e-13 if prec == "double" else 1e-6)
+    assert relerr(c.get_state(), ref) < tol
+    # the forcing injects eps at the step start: energy grows by ~eps*dt - dissipation*dt
+    assert abs(d["time"] - dt) < 1e-12 + 1e-6 * dt
+
+
+def test_source_term(built_lib):
+    """ComputeRHS adds a user Source (NS.py:259), inside and outside the dealiased set."""
+    N = (32, 32, 32)
+    g = Grid(N)
+    uh = random_state(g, seed=8)
+    rng = np.random.default_rng(9)
+    src = g.forward(rng.standard_normal((3,) + N)) * 0.1
+    c = ctx(N, (2 * np.pi,) * 3, "double")
+    c.set_source(src)
+    assert relerr(c.compute_rhs(uh), g.compute_rhs(uh, source=src)) < 1e-11
+    c.set_source(None)
+    assert relerr(c.compute_rhs(uh), g.compute_rhs(uh)) < 1e-11
