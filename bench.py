@@ -37,7 +37,7 @@ METRIC = "RK4 steps/s at 512^3 FP32 vs FP64; closure-LES speedup at spectrum err
 WORKLOAD = ("forced isotropic turbulence 512^3 FP32 (seeded k^4 exp(-2(k/4)^2) field, E=0.5, "
             "eps=0.1 forcing on |k|<=2, nu=8e-4, RK4 CFL 0.5, 2/3 rule)")
 NU, EPS, KF, CFL, K0 = 0.0008, 0.1, 2.0, 0.5, 4.0
-KERNEL_NAMES = ["x_inv_curl", "y_inv", "z_c2r_cross_r2c", "y_fwd", "x_fwd_project_rk4"]
+KERNEL_NAMES = ["x_inv_curl", "y_inv", "z_c2r_cross_r2c", "y_fwd", "x_fwd", "rk_update"]
 
 
 def parse():
@@ -139,7 +139,8 @@ def kernel_bytes(n, csz=8, acc=16):
         "y_inv": 6 * a1 * csz + 6 * a2 * csz,
         "z_c2r_cross_r2c": 6 * n * n * Kz * csz + 3 * a2 * csz,
         "y_fwd": 3 * a2 * csz + 3 * a1 * csz,
-        "x_fwd_project_rk4": 3 * a1 * csz + rk_state,
+        "x_fwd": 3 * a1 * csz + 3 * comp * csz,
+        "rk_update": 3 * comp * csz + rk_state,
     }
 
 

@@ -662,9 +662,21 @@ int launch_stage_sweeps(sdns_ctx* c, const void* yin, int stage, bool cfl_rate, 
   tstart(3);
   CKL(axis_plain(c, d, -1));
   tstop(3);
-  // x forward + projection + diffusion + RK4 stage
+  // x forward: T1 [3][N0][K1][Kzp] -> scaled, masked nonlinear term in the
+  // compact layout [3][K0][K1][Kzp], written into T2 (free after the y sweep)
+  AxisArgs x = {};
+  x.in = c->T1; x.out = c->T2;
+  x.min = c->f0; x.mout = c->m0;
+  x.in_fs = (long long)c->N0 * K1 * Kzp; x.in_ss = 0; x.in_rs = K1 * Kzp;
+  x.out_fs = c->ncomp1; x.out_ss = 0; x.out_rs = K1 * Kzp;
+  x.nlines = K1 * Kzp; x.B = x.nlines; x.nfield = 3; x.scale = 1.0 / ((double)c->N0 * c->N1 * c->N2);
+  x.tw = twp(c, 0);
+  tstart(4);
+  CKL(axis_plain(c, x, -1));
+  tstop(4);
+  // projection + diffusion + source + forcing + RK4 stage update
   RKArgs r = {};
-  r.in = c->T1; r.m0 = c->m0; r.m1 = c->m1; r.Kz = c->Kz; r.Kzp = c->Kzp; r.nlines = K1 * Kzp;
+  r.in = c->T2; r.m0 = c->m0; r.m1 = c->m1; r.Kz = c->Kz; r.Kzp = c->Kzp; r.nlines = K1 * Kzp;
   r.scale = 1.0 / ((double)c->N0 * c->N1 * c->N2); r.tw = twp(c, 0);
   for (int i = 0; i < 3; ++i) r.kscale[i] = c->kscale[i];
   r.nu = c->cfg.nu; r.stage = stage;
@@ -680,9 +692,9 @@ int launch_stage_sweeps(sdns_ctx* c, const void* yin, int stage, bool cfl_rate, 
   r.force_alpha = (c->eps > 0 && stage < 4) ? c->sc + SC_ALPHA : nullptr;
   r.kf2 = c->kf * c->kf;
   r.partials = c->partials;
-  tstart(4);
-  CKL(c->dbl ? Kernels<double>::axis_rk(r, s, nullptr) : Kernels<float>::axis_rk(r, s, nullptr));
-  tstop(4);
+  tstart(5);
+  CKL(c->dbl ? Kernels<double>::rk_update(r, s) : Kernels<float>::rk_update(r, s));
+  tstop(5);
   return SDNS_OK;
 }
 
@@ -786,15 +798,8 @@ int sdns_create(const sdns_config* cfg, sdns_ctx** out) {
   if (cfg->store_pressure && (e = dalloc(c, &c->Pc, c->ncomp1 * cb))) return bail(e);
   if ((e = dalloc(c, &c->sc, SC_COUNT * 8))) return bail(e);
   if ((e = dalloc(c, &c->flag, 16))) return bail(e);
-  c->nblk_rk = c->dbl ? 0 : 0;
-  {
-    // blocks of the RK sweep (for the partial-sum buffer)
-    const long long nl = c->K1 * c->Kzp;
-    const int E = c->N0 >= 1024 ? 32 : 16, G = c->N0 / E;
-    int W = 256 / G;
-    while (W > 1 && (size_t)3 * W * line_ld(c->N0) * c->csz + 2 * W * sizeof(int) + 16 > 200 * 1024) W /= 2;
-    c->nblk_rk = (nl + W - 1) / W;
-  }
+  // blocks of the pointwise RK update (one energy/enstrophy partial pair each)
+  c->nblk_rk = (c->K1 * c->Kzp + 255) / 256 * c->K0;
   if ((e = dalloc(c, &c->partials, 2 * c->nblk_rk * 8))) return bail(e);
   // twiddle tables: per axis, pass tables [r][k] of W_{Ns R}^{r k} (forward)
   {

@@ -216,6 +216,23 @@ __device__ __forceinline__ void line_fft_ld(C* buf, int g, int N, const C* __res
   }
 }
 
+// Same transform with the line length N fixed at compile time: the pass
+// sequence, the strides and the twiddle offsets are constants, so the index
+// arithmetic of every pass folds into immediate offsets.
+template <int N, int E, int S, int Ns, typename C>
+__device__ __forceinline__ void passes_t(C* buf, int g, const C* __restrict__ tw, int off) {
+  if constexpr (Ns < N) {
+    constexpr int R = (N / Ns) >= 16 ? 16 : N / Ns;
+    stockham_pass<R, E, S>(buf, g, N / E, N, Ns, tw + off);
+    passes_t<N, E, S, Ns * R>(buf, g, tw, off + R * Ns);
+  }
+}
+template <int N, int E, int S, typename C, typename Loader>
+__device__ __forceinline__ void line_fft_ld_t(C* buf, int g, const C* __restrict__ tw, Loader& ld) {
+  stockham_first16<E, S>(buf, g, N / E, N, ld);
+  passes_t<N, E, S, 16>(buf, g, tw, 16);
+}
+
 // ---------------------------------------------------------------------------
 // Register-resident ends of a line transform.  After the last Stockham pass
 // the lane g of a group holds the outputs of positions g + G*m, m = 0..E-1,

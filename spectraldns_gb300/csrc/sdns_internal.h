@@ -114,6 +114,7 @@ template <typename Real> struct Kernels {
   static int zline_c2r(const ZArgs& a, cudaStream_t s);
   static int zline_r2c(const ZArgs& a, cudaStream_t s);
   static int axis_rk(const RKArgs& a, cudaStream_t s, int* nblocks_out);
+  static int rk_update(const RKArgs& a, cudaStream_t s);
   static int smem_optin(int dev);
 };
 

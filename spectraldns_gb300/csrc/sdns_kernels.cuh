@@ -32,137 +32,232 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float x) {
 }
 
 // ---------------------------------------------------------------------------
-// strided axis sweep.  MODE 0: out field f = transform of in field f.
-// MODE 1 (inverse x with curl): out fields 0-2 = u_hat, 3-5 = i K x u_hat;
-// the two components of a curl field are staged and combined in the first
-// radix pass.
+// Persistent, double-buffered plain axis sweep (MODE 0 of k_axis).  A task is
+// one tile of W adjacent lines of one field (tasks field-major, so blocks
+// running at the same time stream neighbouring tiles of one field); each
+// block walks tasks blockIdx.x, blockIdx.x + gridDim.x, ... and stages the
+// next task's rows with cp.async while it transforms and stores the current
+// one.  Every thread stages and stores one fixed column (line) of the tile,
+// so the line bases are computed once per task.
 // ---------------------------------------------------------------------------
-template <typename Real, int E, int S, int MODE>
-__global__ void __launch_bounds__(256, 3) k_axis(AxisArgs a) {
+template <int N> struct axis_e { static constexpr int value = N >= 1024 ? 32 : 16; };
+
+template <typename Real, int N, int S>
+__global__ void __launch_bounds__(256, 3) k_axis_p(AxisArgs a) {
   using C = typename cplx_of<Real>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int N = a.min.n;
-  const int G = N / E;
+  constexpr int E = axis_e<N>::value, G = N / E, LD = (N + ((N - 1) >> 4)) | 1;
   const int W = blockDim.x / G;
   const int wsh = __ffs(W) - 1;
-  const int LD = line_ld(N);
-  const int f = blockIdx.y;
-  const int ntile = (MODE == 1) ? 2 : 1;
-  C* t1 = reinterpret_cast<C*>(smraw);
-  C* t2 = t1 + (size_t)W * LD;
-  long long* cin = reinterpret_cast<long long*>(t1 + (size_t)ntile * W * LD);
-  long long* cout = cin + W;
-  Real* ck = reinterpret_cast<Real*>(cout + W);  // k1, kz per column (curl)
-  const long long l0 = (long long)blockIdx.x * W;
+  C* const bufs = reinterpret_cast<C*>(smraw);
   const int tid = threadIdx.x, nth = blockDim.x;
-
-  for (int w = tid; w < W; w += nth) {
-    const long long l = l0 + w;
-    long long bi = -1, bo = -1;
-    if (l < a.nlines) {
-      const long long slab = l / a.B, b = l - slab * a.B;
-      bi = slab * a.in_ss + b;
-      bo = slab * a.out_ss + b;
-      if (MODE == 1) {
-        const int k1row = (int)(b / a.Kzp), kz = (int)(b - (long long)k1row * a.Kzp);
-        ck[2 * w] = (Real)(a.kscale[1] * a.m1.wave(k1row));
-        ck[2 * w + 1] = (Real)(a.kscale[2] * kz);
+  const int lane = tid & 31, warp = tid >> 5;
+  const int wl = warp * (32 / G) + lane / G, g = lane % G;  // FFT phase: line of this lane
+  const int wc = tid & (W - 1), r0 = tid >> wsh;            // staging phase: column, first row (step G)
+  // 32-bit task bookkeeping (the launcher checks nlines * nfield < 2^31)
+  const unsigned nlines = (unsigned)a.nlines, B = (unsigned)a.B;
+  const unsigned ntile = (nlines + W - 1) / W;
+  const unsigned ntask = ntile * (unsigned)a.nfield;
+  const int rin = a.min.rows(), rout = a.mout.rows();
+  const C* in = reinterpret_cast<const C*>(a.in);
+  const C* tw = reinterpret_cast<const C*>(a.tw);
+  const Real sc = (Real)a.scale;
+  auto issue = [&](unsigned f, unsigned tile, C* dst) {
+    const unsigned l = tile * W + wc;
+    if (l < nlines) {
+      const unsigned slab = l / B;
+      const C* src = in + (long long)f * a.in_fs + (long long)slab * a.in_ss + (l - slab * B) + (long long)r0 * a.in_rs;
+      const long long step = (long long)G * a.in_rs;
+      C* d = dst + wc * LD;
+      for (int r = r0; r < rin; r += G, src += step) cp_async<sizeof(C)>(d + padp(r), src);
+    }
+    cp_commit();
+  };
+  const unsigned gstep = gridDim.x;
+  unsigned task = blockIdx.x;
+  unsigned f = task / ntile, tile = task - f * ntile;
+  int b = 0;
+  if (task < ntask) issue(f, tile, bufs);
+  for (; task < ntask; task += gstep, b ^= 1) {
+    C* const cur = bufs + (size_t)b * W * LD;
+    unsigned nf = f, ntl = tile + gstep;
+    while (ntl >= ntile) { ntl -= ntile; ++nf; }
+    if (task + gstep < ntask) {
+      issue(nf, ntl, bufs + (size_t)(b ^ 1) * W * LD);
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    } else {
+      cp_wait_all();
+    }
+    __syncthreads();
+    {
+      C* line = cur + wl * LD;
+      const RowMap mi = a.min;
+      auto ld = [&](int p) -> C {
+        int r = p;
+        if (mi.kc >= 0) {
+          if (p > mi.kc && p < N - mi.kc) return czero<C>();
+          if (p > mi.kc) r = p - N + 2 * mi.kc + 1;
+        }
+        return line[padp(r)];
+      };
+      line_fft_ld_t<N, E, S>(line, g, tw, ld);
+    }
+    __syncthreads();
+    {
+      C* out = reinterpret_cast<C*>(a.out) + (long long)f * a.out_fs;
+      if constexpr (sizeof(C) == 8) {
+        // adjacent line pairs -> one 16-byte store; this thread: columns 2u, 2u+1
+        const int Wh = W >> 1, u = tid % Wh;
+        const unsigned l0 = tile * W + 2 * u;
+        if (l0 < nlines) {
+          const unsigned slab = l0 / B, rem = l0 - slab * B;
+          const long long b0 = (long long)slab * a.out_ss + rem;
+          const bool has1 = l0 + 1 < nlines;
+          const long long b1 = (rem + 1 < B) ? b0 + 1 : (long long)(slab + 1) * a.out_ss;
+          const bool pair = has1 && b1 == b0 + 1 && ((b0 & 1) == 0) && ((a.out_rs & 1) == 0);
+          const C* c0 = cur + (2 * u) * LD;
+          for (int r = tid / Wh; r < rout; r += nth / Wh) {
+            const int pp = padp(a.mout.pos(r));
+            const C v0 = c0[pp];
+            const long long o = r * a.out_rs + b0;
+            if (pair) {
+              const C v1 = c0[LD + pp];
+              reinterpret_cast<float4*>(out)[o >> 1] = make_float4(v0.x * sc, v0.y * sc, v1.x * sc, v1.y * sc);
+            } else {
+              out[o] = mk<C>(v0.x * sc, v0.y * sc);
+              if (has1) {
+                const C v1 = c0[LD + pp];
+                out[r * a.out_rs + b1] = mk<C>(v1.x * sc, v1.y * sc);
+              }
+            }
+          }
+        }
+      } else {
+        const unsigned l = tile * W + wc;
+        if (l < nlines) {
+          const unsigned slab = l / B;
+          const long long bo = (long long)slab * a.out_ss + (l - slab * B);
+          const C* c0 = cur + wc * LD;
+          for (int r = r0; r < rout; r += G) {
+            const C v = c0[padp(a.mout.pos(r))];
+            out[r * a.out_rs + bo] = mk<C>(v.x * sc, v.y * sc);
+          }
+        }
       }
     }
-    cin[w] = bi;
-    cout[w] = bo;
+    __syncthreads();  // cur is refilled two tasks ahead
+    f = nf;
+    tile = ntl;
   }
-  __syncthreads();
+}
 
-  // inputs: MODE 0 field f; MODE 1 curl fields read two components
-  int c1 = f, c2 = -1;
-  if (MODE == 1) {
-    if (f == 3) { c1 = 2; c2 = 1; }       // i (k1 uz - kz uy)
-    else if (f == 4) { c1 = 0; c2 = 2; }  // i (kz ux - k0 uz)
-    else if (f == 5) { c1 = 1; c2 = 0; }  // i (k0 uy - k1 ux)
-  }
-  const int rin = a.min.rows();
+// x^-1 sweep with the curl: one block stages the three velocity components of
+// a tile of W lines once and produces all six output fields from them (u_hat
+// and i K x u_hat), one line transform per warp and field.
+__host__ __device__ inline int staged_rows(int rin) { return ((rin - 1) + ((rin - 1) >> 4) + 2) & ~1; }
+
+template <typename Real, int N>
+__global__ void __launch_bounds__(256, 2) k_axis_curl6(AxisArgs a) {
+  using C = typename cplx_of<Real>::type;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  constexpr int E = axis_e<N>::value, G = N / E, LD = (N + ((N - 1) >> 4)) | 1;
+  const int W = blockDim.x / G;
+  const int wsh = __ffs(W) - 1;
+  const int rin = a.min.rows(), rout = a.mout.rows();
+  const int PR = staged_rows(rin);
+  C* const comp = reinterpret_cast<C*>(smraw);    // [3][W][PR] staged components
+  C* const work = comp + (size_t)3 * W * PR;       // [W][LD] transform buffers
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int wl = warp * (32 / G) + lane / G, g = lane % G;
+  const int wc = tid & (W - 1), r0 = tid >> wsh;
+  const long long tile = blockIdx.x;
   const C* in = reinterpret_cast<const C*>(a.in);
+  const C* tw = reinterpret_cast<const C*>(a.tw);
   {
-    const C* s1 = in + c1 * a.in_fs;
-    const C* s2 = in + (c2 >= 0 ? c2 : 0) * a.in_fs;
-    for (int i = tid; i < rin * W; i += nth) {
-      const int r = i >> wsh, w = i & (W - 1);
-      const long long bi = cin[w];
-      if (bi >= 0) {
-        const long long o = r * a.in_rs + bi;
-        cp_async<sizeof(C)>(&t1[w * LD + padp(r)], s1 + o);
-        if (c2 >= 0) cp_async<sizeof(C)>(&t2[w * LD + padp(r)], s2 + o);
+    const long long l = tile * W + wc;
+    if (l < a.nlines) {
+      const long long step = (long long)G * a.in_rs;
+#pragma unroll 1
+      for (int c = 0; c < 3; ++c) {
+        const C* src = in + c * a.in_fs + l + (long long)r0 * a.in_rs;
+        C* d = comp + (size_t)(c * W + wc) * PR;
+        for (int r = r0; r < rin; r += G, src += step) cp_async<sizeof(C)>(d + padp(r), src);
       }
     }
     cp_commit();
-    cp_wait_all();
   }
-  __syncthreads();
+  // wave numbers of this lane's line: b = k1row * Kzp + kz
+  Real k1 = 0, kz = 0;
   {
-    const int lane = tid & 31, warp = tid >> 5;
-    const int w = warp * (32 / G) + lane / G;
-    C* line = t1 + w * LD;
-    const C* line2 = t2 + w * LD;
-    const RowMap mi = a.min;
-    const Real k1 = (MODE == 1) ? ck[2 * w] : (Real)0, kz = (MODE == 1) ? ck[2 * w + 1] : (Real)0;
-    const Real ks0 = (Real)a.kscale[0];
-    const int fm = f;
+    const long long l = tile * W + wl;
+    if (l < a.nlines) {
+      const int k1row = (int)(l / a.Kzp);
+      k1 = (Real)(a.kscale[1] * a.m1.wave(k1row));
+      kz = (Real)(a.kscale[2] * (double)(l - (long long)k1row * a.Kzp));
+    }
+  }
+  const Real ks0 = (Real)a.kscale[0];
+  const RowMap mi = a.min;
+  cp_wait_all();
+  __syncthreads();
+#pragma unroll 1
+  for (int f = 0; f < 6; ++f) {
+    C* line = work + wl * LD;
+    int c1 = f, c2 = 0;
+    if (f == 3) { c1 = 2; c2 = 1; }       // i (k1 uz - kz uy)
+    else if (f == 4) { c1 = 0; c2 = 2; }  // i (kz ux - k0 uz)
+    else if (f == 5) { c1 = 1; c2 = 0; }  // i (k0 uy - k1 ux)
+    const C* s1 = comp + (size_t)(c1 * W + wl) * PR;
+    const C* s2 = comp + (size_t)(c2 * W + wl) * PR;
     auto ld = [&](int p) -> C {
       int r = p;
       if (mi.kc >= 0) {
         if (p > mi.kc && p < N - mi.kc) return czero<C>();
         if (p > mi.kc) r = p - N + 2 * mi.kc + 1;
       }
-      const C v1 = line[padp(r)];
-      if (MODE == 0 || fm < 3) return v1;
-      const C v2 = line2[padp(r)];
+      const C v1 = s1[padp(r)];
+      if (f < 3) return v1;
+      const C v2 = s2[padp(r)];
       C t;
-      if (fm == 3) {
+      if (f == 3) {
         t = mk<C>(k1 * v1.x - kz * v2.x, k1 * v1.y - kz * v2.y);
       } else {
         const Real k0 = ks0 * (Real)mi.wave(r);
-        if (fm == 4) t = mk<C>(kz * v1.x - k0 * v2.x, kz * v1.y - k0 * v2.y);
+        if (f == 4) t = mk<C>(kz * v1.x - k0 * v2.x, kz * v1.y - k0 * v2.y);
         else t = mk<C>(k0 * v1.x - k1 * v2.x, k0 * v1.y - k1 * v2.y);
       }
       return mk<C>(-t.y, t.x);
     };
-    line_fft_ld<E, S>(line, lane % G, N, reinterpret_cast<const C*>(a.tw), ld);
-  }
-  __syncthreads();
-  const int rout = a.mout.rows();
-  C* out = reinterpret_cast<C*>(a.out) + f * a.out_fs;
-  const Real sc = (Real)a.scale;
-  if (sizeof(C) == 8) {
-    // pairs of adjacent lines -> one 16-byte store
-    const int Wh = W >> 1;
-    for (int i = tid; i < rout * Wh; i += nth) {
-      const int r = i / Wh, w = (i - r * Wh) * 2;
-      const long long b0 = cout[w], b1 = cout[w + 1];
-      if (b0 < 0) continue;
-      const int pp = padp(a.mout.pos(r));
-      const C v0 = t1[w * LD + pp];
-      const long long o = r * a.out_rs + b0;
-      if (b1 == b0 + 1 && ((o & 1) == 0)) {
-        const C v1 = t1[(w + 1) * LD + pp];
-        reinterpret_cast<float4*>(out)[o >> 1] = make_float4(v0.x * sc, v0.y * sc, v1.x * sc, v1.y * sc);
-      } else {
-        out[o] = mk<C>(v0.x * sc, v0.y * sc);
-        if (b1 >= 0) {
-          const C v1 = t1[(w + 1) * LD + pp];
-          out[r * a.out_rs + b1] = mk<C>(v1.x * sc, v1.y * sc);
+    line_fft_ld_t<N, E, 1>(line, g, tw, ld);
+    __syncthreads();
+    C* out = reinterpret_cast<C*>(a.out) + f * a.out_fs;
+    if constexpr (sizeof(C) == 8) {
+      const int Wh = W >> 1, u = tid % Wh;
+      const long long l0 = tile * W + 2 * u;
+      if (l0 < a.nlines) {
+        const bool pair = l0 + 1 < a.nlines;  // l0 even, a.B = nlines and out_rs even: 16-byte aligned pair
+        const C* c0 = work + (2 * u) * LD;
+        for (int r = tid / Wh; r < rout; r += nth / Wh) {
+          const int pp = padp(a.mout.pos(r));
+          const C v0 = c0[pp];
+          const long long o = r * a.out_rs + l0;
+          if (pair) {
+            const C v1 = c0[LD + pp];
+            reinterpret_cast<float4*>(out)[o >> 1] = make_float4(v0.x, v0.y, v1.x, v1.y);
+          } else {
+            out[o] = v0;
+          }
         }
       }
-    }
-  } else {
-    for (int i = tid; i < rout * W; i += nth) {
-      const int r = i >> wsh, w = i & (W - 1);
-      const long long bo = cout[w];
-      if (bo >= 0) {
-        const C v = t1[w * LD + padp(a.mout.pos(r))];
-        out[r * a.out_rs + bo] = mk<C>(v.x * sc, v.y * sc);
+    } else {
+      const long long l = tile * W + wc;
+      if (l < a.nlines) {
+        const C* c0 = work + wc * LD;
+        for (int r = r0; r < rout; r += G) out[r * a.out_rs + l] = c0[padp(a.mout.pos(r))];
       }
     }
+    __syncthreads();
   }
 }
 
@@ -670,40 +765,295 @@ __global__ void __launch_bounds__(256, 2) k_axis_rk(RKArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Pointwise end of a stage after the x forward sweep (which wrote the scaled,
+// masked nonlinear term in the compact layout to a.in): pressure projection,
+// diffusion, source, forcing and the RK4 stage update, one thread per mode.
+// Grid: x over b = k1row*Kzp + kz (blockDim.x modes per block), y over the
+// compact rows of axis 0.  Stage 3 also writes per-block energy and
+// enstrophy partial sums of the new state (block id y*gridDim.x + x).
+// ---------------------------------------------------------------------------
+// error-free sum of two float-float numbers (hi, lo) += (h2, l2)
+__device__ __forceinline__ void ff_add2(float& hi, float& lo, float h2, float l2) {
+  const float s = __fadd_rn(hi, h2);
+  const float bb = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(h2, bb));
+  const float t = __fadd_rn(__fadd_rn(e, lo), l2);
+  hi = __fadd_rn(s, t);
+  lo = __fsub_rn(t, __fsub_rn(hi, s));
+}
+
+// block sum of per-thread values; FP32 values are summed as float-float
+// (compensated), FP64 values directly.  Valid in thread 0.
+__device__ __forceinline__ double block_sum2(float x, float y, double* red, double& ys) {
+  float xh = x, xl = 0.f, yh = y, yl = 0.f;
+  for (int q = 16; q > 0; q >>= 1) {
+    const float a0 = __shfl_xor_sync(0xffffffffu, xh, q), a1 = __shfl_xor_sync(0xffffffffu, xl, q);
+    const float b0 = __shfl_xor_sync(0xffffffffu, yh, q), b1 = __shfl_xor_sync(0xffffffffu, yl, q);
+    ff_add2(xh, xl, a0, a1);
+    ff_add2(yh, yl, b0, b1);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[2 * warp] = (double)xh + (double)xl;
+    red[2 * warp + 1] = (double)yh + (double)yl;
+  }
+  __syncthreads();
+  double xs = 0;
+  ys = 0;
+  if (threadIdx.x == 0)
+    for (int q = 0; q < (int)(blockDim.x + 31) / 32; ++q) { xs += red[2 * q]; ys += red[2 * q + 1]; }
+  return xs;
+}
+__device__ __forceinline__ double block_sum2(double x, double y, double* red, double& ys) {
+  for (int q = 16; q > 0; q >>= 1) {
+    x += __shfl_xor_sync(0xffffffffu, x, q);
+    y += __shfl_xor_sync(0xffffffffu, y, q);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { red[2 * warp] = x; red[2 * warp + 1] = y; }
+  __syncthreads();
+  double xs = 0;
+  ys = 0;
+  if (threadIdx.x == 0)
+    for (int q = 0; q < (int)(blockDim.x + 31) / 32; ++q) { xs += red[2 * q]; ys += red[2 * q + 1]; }
+  return xs;
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(256) k_rk_update(RKArgs a) {
+  using C = typename cplx_of<Real>::type;
+  using AT = typename Acc<Real>::T;
+  __shared__ double red[16];
+  __shared__ Real coef[3];  // b dt, a dt, forcing alpha of this stage
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    const double dt = *a.dt;
+    coef[0] = (Real)(a.b * dt);
+    coef[1] = (Real)(a.a * dt);
+    coef[2] = (Real)(a.force_alpha ? *a.force_alpha : 0.0);
+  }
+  __syncthreads();
+  const long long nl = a.nlines;
+  const int r = blockIdx.y;
+  const long long bi = (long long)blockIdx.x * blockDim.x + tid;
+  const int K0 = a.m0.rows();
+  const long long cs = (long long)K0 * nl;  // component stride of the compact layout
+  const int stage = a.stage;
+  Real e_sum = 0, z_sum = 0;
+  if (bi < nl) {
+    const int k1row = (int)((unsigned)bi / (unsigned)a.Kzp), kz = (int)bi - k1row * a.Kzp;
+    const long long o = (long long)r * nl + bi;
+    C* Y = reinterpret_cast<C*>(a.Y);
+    AT* Sg = reinterpret_cast<AT*>(a.S);
+    AT* Ag = reinterpret_cast<AT*>(a.A);
+    const C* nlp = reinterpret_cast<const C*>(a.in);
+    if (kz >= a.Kz) {  // padding of the R2C axis stays zero
+      AT z0;
+      memset(&z0, 0, sizeof(z0));
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (stage == 4) {
+          reinterpret_cast<C*>(a.rhs_out)[c * cs + o] = czero<C>();
+        } else {
+          Y[c * cs + o] = czero<C>();
+          if (stage == 3) Sg[c * cs + o] = z0; else Ag[c * cs + o] = z0;
+        }
+      }
+      if (a.p_out) reinterpret_cast<C*>(a.p_out)[o] = czero<C>();
+    } else {
+      const Real bdt = coef[0], adt = coef[1], alph = coef[2];
+      const Real k[3] = {(Real)a.kscale[0] * (Real)a.m0.wave(r), (Real)a.kscale[1] * (Real)a.m1.wave(k1row),
+                         (Real)a.kscale[2] * (Real)kz};
+      const Real K2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+      const bool forced = a.force_alpha && K2 > (Real)0 && K2 <= (Real)a.kf2;
+      const bool need_s = stage <= 2 || forced;
+      const bool need_a = stage >= 1 && stage <= 3;
+      const AT* src = reinterpret_cast<const AT*>(a.source);
+      // every load of this mode is issued before the first store
+      C nlv[3], uv[3];
+      AT sv[3], av[3], qv[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const long long oc = c * cs + o;
+        nlv[c] = nlp[oc];
+        memset(&sv[c], 0, sizeof(AT));
+        memset(&av[c], 0, sizeof(AT));
+        memset(&qv[c], 0, sizeof(AT));
+        if (need_s) sv[c] = Sg[oc];
+        if (need_a) av[c] = Ag[oc];
+        if (stage != 0) uv[c] = Y[oc];
+        if (src) qv[c] = src[oc];
+      }
+      const Real iK2 = K2 > (Real)0 ? (Real)1 / K2 : (Real)0;
+      const C P = mk<C>((nlv[0].x * k[0] + nlv[1].x * k[1] + nlv[2].x * k[2]) * iK2,
+                        (nlv[0].y * k[0] + nlv[1].y * k[1] + nlv[2].y * k[2]) * iK2);
+      if (a.p_out) reinterpret_cast<C*>(a.p_out)[o] = P;
+      const Real nuK2 = (Real)a.nu * K2;
+      Real snx[3] = {0, 0, 0}, sny[3] = {0, 0, 0};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const long long oc = c * cs + o;
+        const AT s = sv[c];
+        AT acc = av[c];
+        const C u = stage == 0 ? mk<C>((Real)s.x, (Real)s.y) : uv[c];
+        C rhs = mk<C>(nlv[c].x - P.x * k[c] - nuK2 * u.x, nlv[c].y - P.y * k[c] - nuK2 * u.y);
+        if (src) { rhs.x += (Real)qv[c].x; rhs.y += (Real)qv[c].y; }
+        if (forced) { rhs.x += alph * (Real)s.x; rhs.y += alph * (Real)s.y; }
+        if (stage == 4) {
+          reinterpret_cast<C*>(a.rhs_out)[oc] = rhs;
+          continue;
+        }
+        if (stage == 0) acc = s;
+        if constexpr (sizeof(Real) == 4) {
+          // compensated FP32: Y' = S + b dt rhs ; A' = (S or A) + a dt rhs
+          if (stage < 3) {
+            float yx = s.x, ylx = s.z, yy = s.y, yly = s.w;
+            ff_add(yx, ylx, bdt * rhs.x);
+            ff_add(yy, yly, bdt * rhs.y);
+            Y[oc] = mk<C>(yx, yy);
+            ff_add(acc.x, acc.z, adt * rhs.x);
+            ff_add(acc.y, acc.w, adt * rhs.y);
+            Ag[oc] = acc;
+          } else {
+            ff_add(acc.x, acc.z, adt * rhs.x);
+            ff_add(acc.y, acc.w, adt * rhs.y);
+            Sg[oc] = acc;
+            Y[oc] = mk<C>(acc.x, acc.y);
+            snx[c] = acc.x;
+            sny[c] = acc.y;
+          }
+        } else {
+          if (stage < 3) {
+            Y[oc] = mk<C>(s.x + bdt * rhs.x, s.y + bdt * rhs.y);
+            acc.x += adt * rhs.x;
+            acc.y += adt * rhs.y;
+            Ag[oc] = acc;
+          } else {
+            acc.x += adt * rhs.x;
+            acc.y += adt * rhs.y;
+            Sg[oc] = acc;
+            Y[oc] = mk<C>(acc.x, acc.y);
+            snx[c] = (Real)acc.x;
+            sny[c] = (Real)acc.y;
+          }
+        }
+      }
+      if (stage == 3) {
+        const Real wz = (kz == 0) ? (Real)0.5 : (Real)1;  // 1/2 * Hermitian weight
+        const Real e = snx[0] * snx[0] + sny[0] * sny[0] + snx[1] * snx[1] + sny[1] * sny[1] + snx[2] * snx[2] +
+                       sny[2] * sny[2];
+        const Real cxr = k[1] * snx[2] - k[2] * snx[1], cxi = k[1] * sny[2] - k[2] * sny[1];
+        const Real cyr = k[2] * snx[0] - k[0] * snx[2], cyi = k[2] * sny[0] - k[0] * sny[2];
+        const Real czr = k[0] * snx[1] - k[1] * snx[0], czi = k[0] * sny[1] - k[1] * sny[0];
+        const Real z = cxr * cxr + cxi * cxi + cyr * cyr + cyi * cyi + czr * czr + czi * czi;
+        e_sum = wz * e;
+        z_sum = wz * z;
+      }
+    }
+  }
+  if (stage == 3 && a.partials) {
+    double zs;
+    const double es = block_sum2(e_sum, z_sum, red, zs);
+    if (tid == 0) {
+      const long long blk = (long long)blockIdx.y * gridDim.x + blockIdx.x;
+      a.partials[2 * blk] = es;
+      a.partials[2 * blk + 1] = zs;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 inline int elems_for(int n) { return n >= 1024 ? 32 : 16; }
 
-template <typename Real>
-static size_t axis_smem(int n, int W, bool curl) {
-  using C = typename cplx_of<Real>::type;
-  return (size_t)(curl ? 2 : 1) * W * line_ld(n) * sizeof(C) + 2 * W * sizeof(long long) +
-         (curl ? 2 * W * sizeof(Real) : 0) + 16;
+// lines per tile of the shared-memory sweeps: 256 threads' worth, halved
+// while the tile does not fit the opt-in shared memory of a block
+inline int fit_width(int G, size_t per_line, size_t fixed, size_t limit) {
+  int W = 256 / G;
+  while (W > 2 && fixed + (size_t)W * per_line > limit) W >>= 1;
+  return W;
+}
+inline size_t smem_limit() {
+  int dev = 0, mx = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return (size_t)mx - 1024;  // static shared memory of the kernels stays below 1 KB
 }
 
-template <typename Real, int E, int S, int MODE>
-static int launch_axis(const AxisArgs& a, cudaStream_t s) {
-  const int G = a.min.n / E;
-  const int W = 256 / G;
-  const size_t sm = axis_smem<Real>(a.min.n, W, MODE == 1);
-  auto kern = k_axis<Real, E, S, MODE>;
-  dim3 grid((unsigned)((a.nlines + W - 1) / W), (unsigned)a.nfield, 1);
-  kern<<<grid, 256, sm, s>>>(a);
+template <typename Real, int N, int S>
+static int launch_axis_p(const AxisArgs& a, cudaStream_t s) {
+  using C = typename cplx_of<Real>::type;
+  constexpr int G = N / axis_e<N>::value;
+  const size_t per_line = (size_t)2 * line_ld(N) * sizeof(C);
+  const int W = fit_width(G, per_line, 0, smem_limit());
+  const size_t sm = (size_t)W * per_line;
+  auto kern = k_axis_p<Real, N, S>;
+  int dev = 0, nsm = 148, occ = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, W * G, sm);
+  if (occ < 1) occ = 1;
+  const long long ntask = (a.nlines + W - 1) / W * a.nfield;
+  if (a.nlines * a.nfield >= (1LL << 31) || a.B < 1) return (int)cudaErrorInvalidValue;
+  long long nb = (long long)occ * nsm;
+  if (nb > ntask) nb = ntask;
+  if (nb < 1) return 0;
+  kern<<<(unsigned)nb, W * G, sm, s>>>(a);
   return (int)cudaGetLastError();
+}
+
+template <typename Real, int S>
+static int axis_p_n(const AxisArgs& a, cudaStream_t s) {
+  switch (a.min.n) {
+    case 16: return launch_axis_p<Real, 16, S>(a, s);
+    case 32: return launch_axis_p<Real, 32, S>(a, s);
+    case 64: return launch_axis_p<Real, 64, S>(a, s);
+    case 128: return launch_axis_p<Real, 128, S>(a, s);
+    case 256: return launch_axis_p<Real, 256, S>(a, s);
+    case 512: return launch_axis_p<Real, 512, S>(a, s);
+    case 1024: return launch_axis_p<Real, 1024, S>(a, s);
+    default: return (int)cudaErrorInvalidValue;
+  }
 }
 
 template <typename Real>
 int Kernels<Real>::axis_plain(const AxisArgs& a, int sign, cudaStream_t s) {
-  const int E = elems_for(a.min.n);
-  if (E == 16) return sign < 0 ? launch_axis<Real, 16, -1, 0>(a, s) : launch_axis<Real, 16, 1, 0>(a, s);
-  return sign < 0 ? launch_axis<Real, 32, -1, 0>(a, s) : launch_axis<Real, 32, 1, 0>(a, s);
+  return sign < 0 ? axis_p_n<Real, -1>(a, s) : axis_p_n<Real, 1>(a, s);
+}
+
+template <typename Real, int N>
+static int launch_curl6(const AxisArgs& a, cudaStream_t s) {
+  using C = typename cplx_of<Real>::type;
+  // the x sweep reads lines l at in + c*in_fs + l (one run of lines per field)
+  if (a.B != a.nlines || a.in_ss != 0 || a.out_ss != 0 || a.nfield != 6 || (a.out_rs & 1)) return (int)cudaErrorInvalidValue;
+  constexpr int G = N / axis_e<N>::value;
+  const size_t per_line = ((size_t)3 * staged_rows(a.min.rows()) + line_ld(N)) * sizeof(C);
+  const int W = fit_width(G, per_line, 0, smem_limit());
+  const size_t sm = (size_t)W * per_line;
+  k_axis_curl6<Real, N><<<(unsigned)((a.nlines + W - 1) / W), W * G, sm, s>>>(a);
+  return (int)cudaGetLastError();
 }
 
 template <typename Real>
 int Kernels<Real>::axis_curl_inv(const AxisArgs& a, cudaStream_t s) {
-  const int E = elems_for(a.min.n);
-  if (E == 16) return launch_axis<Real, 16, 1, 1>(a, s);
-  return launch_axis<Real, 32, 1, 1>(a, s);
+  switch (a.min.n) {
+    case 16: return launch_curl6<Real, 16>(a, s);
+    case 32: return launch_curl6<Real, 32>(a, s);
+    case 64: return launch_curl6<Real, 64>(a, s);
+    case 128: return launch_curl6<Real, 128>(a, s);
+    case 256: return launch_curl6<Real, 256>(a, s);
+    case 512: return launch_curl6<Real, 512>(a, s);
+    case 1024: return launch_curl6<Real, 1024>(a, s);
+    default: return (int)cudaErrorInvalidValue;
+  }
+}
+
+template <typename Real>
+int Kernels<Real>::rk_update(const RKArgs& a, cudaStream_t s) {
+  const dim3 grid((unsigned)((a.nlines + 255) / 256), (unsigned)a.m0.rows());
+  k_rk_update<Real><<<grid, 256, 0, s>>>(a);
+  return (int)cudaGetLastError();
 }
 
 template <typename Real, int E>
@@ -820,8 +1170,9 @@ int Kernels<Real>::smem_optin(int dev) {
   int mx = 0;
   cudaError_t e = cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
 #define SDNS_OPT(k) if (e == cudaSuccess) e = optin_one(k, mx)
-  SDNS_OPT((k_axis<Real, 16, -1, 0>)); SDNS_OPT((k_axis<Real, 16, 1, 0>)); SDNS_OPT((k_axis<Real, 16, 1, 1>));
-  SDNS_OPT((k_axis<Real, 32, -1, 0>)); SDNS_OPT((k_axis<Real, 32, 1, 0>)); SDNS_OPT((k_axis<Real, 32, 1, 1>));
+#define SDNS_OPT_N(n) SDNS_OPT((k_axis_p<Real, n, -1>)); SDNS_OPT((k_axis_p<Real, n, 1>)); SDNS_OPT((k_axis_curl6<Real, n>))
+  SDNS_OPT_N(16); SDNS_OPT_N(32); SDNS_OPT_N(64); SDNS_OPT_N(128); SDNS_OPT_N(256); SDNS_OPT_N(512); SDNS_OPT_N(1024);
+#undef SDNS_OPT_N
   SDNS_OPT((k_zline_ns<Real, 16>)); SDNS_OPT((k_zline_ns<Real, 32>));
   SDNS_OPT((k_zline_ns_t<Real, 16>)); SDNS_OPT((k_zline_ns_t<Real, 32>)); SDNS_OPT((k_zline_ns_t<Real, 64>));
   SDNS_OPT((k_zline_ns_t<Real, 128>)); SDNS_OPT((k_zline_ns_t<Real, 256>)); SDNS_OPT((k_zline_ns_t<Real, 512>));
