@@ -394,7 +394,7 @@ __host__ __device__ inline size_t znsr_per_warp(int LD, int Kzp, int LPW) {
 // three inverse ones as conj(fwd(conj(x))), the pack folded into the first
 // radix pass, the unpack done with warp shuffles).
 template <typename Real, int N>
-__global__ void __launch_bounds__(64, 6) k_zline_ns_t(ZArgs a) {
+__global__ void __launch_bounds__(64, 4) k_zline_ns_t(ZArgs a) {
   constexpr int E = 16, G = N / E, LPW = 32 / G;
   using C = typename cplx_of<Real>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
