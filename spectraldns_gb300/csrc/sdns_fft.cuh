@@ -216,6 +216,121 @@ __device__ __forceinline__ void line_fft_ld(C* buf, int g, int N, const C* __res
   }
 }
 
+// ---------------------------------------------------------------------------
+// Passes with the line length N and the stride Ns known at compile time.
+// For p = a + 16 m the padded index is padp(a) + 17 m, so an access pattern
+// j + r*D with D a multiple of 16 needs one padded base per butterfly and
+// constant offsets r*(D + D/16) instead of a shift and an add per access.
+// ---------------------------------------------------------------------------
+template <int D> __device__ __forceinline__ constexpr int pstride() { return D + D / 16; }
+
+// padded index of j = g + G q
+template <int G> __device__ __forceinline__ int padq(int g, int q) {
+  if constexpr (G % 16 == 0) return padp(g) + q * pstride<G>();
+  else return padp(g + G * q);
+}
+
+// position j + r*D, r = 0..R-1, of a line in `buf` (padded); pj = padp(j)
+template <int R, int D, typename C>
+__device__ __forceinline__ void load_r(const C* buf, int j, int pj, C* v) {
+  if constexpr (D % 16 == 0) {
+    const C* b = buf + pj;
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = b[r * pstride<D>()];
+  } else {
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = buf[padp(j + r * D)];
+  }
+}
+template <int R, int D, typename C>
+__device__ __forceinline__ void store_r(C* buf, int j, const C* v) {
+  if constexpr (D % 16 == 0) {
+    C* b = buf + padp(j);
+#pragma unroll
+    for (int r = 0; r < R; ++r) b[r * pstride<D>()] = v[r];
+  } else {
+#pragma unroll
+    for (int r = 0; r < R; ++r) buf[padp(j + r * D)] = v[r];
+  }
+}
+
+template <int R, int E, int S, int N, int Ns, typename C>
+__device__ __forceinline__ void stockham_pass_c(C* buf, int g, const C* __restrict__ tw) {
+  constexpr int G = N / E, NB = E / R, NR = N / R;
+  C v[E];
+#pragma unroll
+  for (int q = 0; q < NB; ++q) load_r<R, NR>(buf, g + G * q, padq<G>(g, q), &v[q * R]);
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const int j = g + G * q;
+    const int k = j & (Ns - 1);
+    if constexpr (Ns > 1) {
+      const C* t = tw + k;
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        C w = t[r * Ns];
+        if (S > 0) w.y = -w.y;
+        v[q * R + r] = cmul(v[q * R + r], w);
+      }
+    }
+    dftR<R, S>(&v[q * R]);
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const int j = g + G * q;
+    const int k = j & (Ns - 1);
+    store_r<R, Ns>(buf, (j - k) * R + k, &v[q * R]);
+  }
+  __syncwarp();
+}
+
+template <int R, int E, int S, int N, int Ns, typename C>
+__device__ __forceinline__ void last_pass_regs_c(const C* buf, int g, const C* __restrict__ tw, C (&x)[E]) {
+  constexpr int G = N / E, NB = E / R, NR = N / R;
+  C v[E];
+#pragma unroll
+  for (int q = 0; q < NB; ++q) load_r<R, NR>(buf, g + G * q, padq<G>(g, q), &v[q * R]);
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const C* t = tw + (g + G * q);  // j < Ns in the last pass, so (j mod Ns) = j
+#pragma unroll
+    for (int r = 1; r < R; ++r) {
+      C w = t[r * Ns];
+      if (S > 0) w.y = -w.y;
+      v[q * R + r] = cmul(v[q * R + r], w);
+    }
+    dftR<R, S>(&v[q * R]);
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q)
+#pragma unroll
+    for (int r = 0; r < R; ++r) x[q + r * NB] = v[q * R + r];
+}
+
+// first radix-16 pass fed by a loader; result written in natural order
+template <int E, int S, int N, typename C, typename Loader>
+__device__ __forceinline__ void first16_c(C* buf, int g, Loader& ld) {
+  constexpr int R = 16, NB = E / R, NR = N / R, G = N / E;
+  C v[E];
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const int j = g + G * q;
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[q * R + r] = ld(j + r * NR);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < NB; ++q) dftR<R, S>(&v[q * R]);
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    C* b = buf + 17 * (g + G * q);  // padp(16 j + r) = 17 j + r for r < 16
+#pragma unroll
+    for (int r = 0; r < R; ++r) b[r] = v[q * R + r];
+  }
+  __syncwarp();
+}
+
 // Same transform with the line length N fixed at compile time: the pass
 // sequence, the strides and the twiddle offsets are constants, so the index
 // arithmetic of every pass folds into immediate offsets.
@@ -223,13 +338,13 @@ template <int N, int E, int S, int Ns, typename C>
 __device__ __forceinline__ void passes_t(C* buf, int g, const C* __restrict__ tw, int off) {
   if constexpr (Ns < N) {
     constexpr int R = (N / Ns) >= 16 ? 16 : N / Ns;
-    stockham_pass<R, E, S>(buf, g, N / E, N, Ns, tw + off);
+    stockham_pass_c<R, E, S, N, Ns>(buf, g, tw + off);
     passes_t<N, E, S, Ns * R>(buf, g, tw, off + R * Ns);
   }
 }
 template <int N, int E, int S, typename C, typename Loader>
 __device__ __forceinline__ void line_fft_ld_t(C* buf, int g, const C* __restrict__ tw, Loader& ld) {
-  stockham_first16<E, S>(buf, g, N / E, N, ld);
+  first16_c<E, S, N>(buf, g, ld);
   passes_t<N, E, S, 16>(buf, g, tw, 16);
 }
 
@@ -343,9 +458,9 @@ __device__ __forceinline__ void fwd_passes_const(C* buf, int g, const C* __restr
   constexpr int G = N / 16;
   constexpr int R = (N / Ns) >= 16 ? 16 : N / Ns;
   if constexpr (Ns * R == N) {
-    last_pass_regs<R, 16, -1>(buf, g, G, N, Ns, tw + off, x);
+    last_pass_regs_c<R, 16, -1, N, Ns>(buf, g, tw + off, x);
   } else {
-    stockham_pass<R, 16, -1>(buf, g, G, N, Ns, tw + off);
+    stockham_pass_c<R, 16, -1, N, Ns>(buf, g, tw + off);
     fwd_passes_const<N, Ns * R>(buf, g, tw, off + R * Ns, x);
   }
 }
@@ -355,8 +470,9 @@ __device__ __forceinline__ void fwd_line_regs(C* buf, int g, const C* __restrict
   dft16<-1>(x);
   if constexpr (N > 16) {
     __syncwarp();  // earlier readers of buf are done
+    C* b = buf + 17 * g;  // padp(16 g + r) = 17 g + r
 #pragma unroll
-    for (int r = 0; r < 16; ++r) buf[padp(g * 16 + r)] = x[r];
+    for (int r = 0; r < 16; ++r) b[r] = x[r];
     __syncwarp();
     fwd_passes_const<N, 16>(buf, g, tw, 16, x);
   }

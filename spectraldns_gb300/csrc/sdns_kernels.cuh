@@ -42,12 +42,27 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float x) {
 // ---------------------------------------------------------------------------
 template <int N> struct axis_e { static constexpr int value = N >= 1024 ? 32 : 16; };
 
+// Pitch (in complex values) of a tile of W lines in shared memory, at least
+// `minlen`.  The staging and store phases access the tile row by row, W
+// lines wide; one shared-memory wavefront serves L = 128/csz lanes.  With
+// W >= L the L lanes hit L lines of one row (odd pitch: distinct banks); with
+// W < L they hit L/W rows of W lines, distinct when pitch = L/W (mod L).
+__host__ __device__ inline int tile_pitch(int minlen, int W, int csz) {
+  const int L = 128 / csz;
+  int ld = minlen;
+  if (W >= L) return ld | 1;
+  const int want = L / W;
+  while ((ld & (L - 1)) != want) ++ld;
+  return ld;
+}
+__host__ __device__ inline int axis_ld(int n, int W, int csz) { return tile_pitch(n + ((n - 1) >> 4), W, csz); }
+
 template <typename Real, int N, int S>
 __global__ void __launch_bounds__(256, 3) k_axis_p(AxisArgs a) {
   using C = typename cplx_of<Real>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
-  constexpr int E = axis_e<N>::value, G = N / E, LD = (N + ((N - 1) >> 4)) | 1;
-  const int W = blockDim.x / G;
+  constexpr int E = axis_e<N>::value, G = N / E;
+  const int W = blockDim.x / G, LD = axis_ld(N, W, (int)sizeof(C));
   const int wsh = __ffs(W) - 1;
   C* const bufs = reinterpret_cast<C*>(smraw);
   const int tid = threadIdx.x, nth = blockDim.x;
@@ -154,17 +169,19 @@ __global__ void __launch_bounds__(256, 3) k_axis_p(AxisArgs a) {
 // x^-1 sweep with the curl: one block stages the three velocity components of
 // a tile of W lines once and produces all six output fields from them (u_hat
 // and i K x u_hat), one line transform per warp and field.
-__host__ __device__ inline int staged_rows(int rin) { return ((rin - 1) + ((rin - 1) >> 4) + 2) & ~1; }
+__host__ __device__ inline int staged_rows(int rin, int W, int csz) {
+  return tile_pitch((rin - 1) + ((rin - 1) >> 4) + 1, W, csz);
+}
 
 template <typename Real, int N>
 __global__ void __launch_bounds__(256, 2) k_axis_curl6(AxisArgs a) {
   using C = typename cplx_of<Real>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
-  constexpr int E = axis_e<N>::value, G = N / E, LD = (N + ((N - 1) >> 4)) | 1;
-  const int W = blockDim.x / G;
+  constexpr int E = axis_e<N>::value, G = N / E;
+  const int W = blockDim.x / G, LD = axis_ld(N, W, (int)sizeof(C));
   const int wsh = __ffs(W) - 1;
   const int rin = a.min.rows(), rout = a.mout.rows();
-  const int PR = staged_rows(rin);
+  const int PR = staged_rows(rin, W, (int)sizeof(C));
   C* const comp = reinterpret_cast<C*>(smraw);    // [3][W][PR] staged components
   C* const work = comp + (size_t)3 * W * PR;       // [W][LD] transform buffers
   const int tid = threadIdx.x, nth = blockDim.x;
@@ -967,13 +984,6 @@ __global__ void __launch_bounds__(256) k_rk_update(RKArgs a) {
 // ---------------------------------------------------------------------------
 inline int elems_for(int n) { return n >= 1024 ? 32 : 16; }
 
-// lines per tile of the shared-memory sweeps: 256 threads' worth, halved
-// while the tile does not fit the opt-in shared memory of a block
-inline int fit_width(int G, size_t per_line, size_t fixed, size_t limit) {
-  int W = 256 / G;
-  while (W > 2 && fixed + (size_t)W * per_line > limit) W >>= 1;
-  return W;
-}
 inline size_t smem_limit() {
   int dev = 0, mx = 0;
   cudaGetDevice(&dev);
@@ -985,9 +995,10 @@ template <typename Real, int N, int S>
 static int launch_axis_p(const AxisArgs& a, cudaStream_t s) {
   using C = typename cplx_of<Real>::type;
   constexpr int G = N / axis_e<N>::value;
-  const size_t per_line = (size_t)2 * line_ld(N) * sizeof(C);
-  const int W = fit_width(G, per_line, 0, smem_limit());
-  const size_t sm = (size_t)W * per_line;
+  const size_t lim = smem_limit();
+  int W = 256 / G;
+  while (W > 2 && (size_t)2 * W * axis_ld(N, W, (int)sizeof(C)) * sizeof(C) > lim) W >>= 1;
+  const size_t sm = (size_t)2 * W * axis_ld(N, W, (int)sizeof(C)) * sizeof(C);
   auto kern = k_axis_p<Real, N, S>;
   int dev = 0, nsm = 148, occ = 1;
   cudaGetDevice(&dev);
@@ -1028,9 +1039,14 @@ static int launch_curl6(const AxisArgs& a, cudaStream_t s) {
   // the x sweep reads lines l at in + c*in_fs + l (one run of lines per field)
   if (a.B != a.nlines || a.in_ss != 0 || a.out_ss != 0 || a.nfield != 6 || (a.out_rs & 1)) return (int)cudaErrorInvalidValue;
   constexpr int G = N / axis_e<N>::value;
-  const size_t per_line = ((size_t)3 * staged_rows(a.min.rows()) + line_ld(N)) * sizeof(C);
-  const int W = fit_width(G, per_line, 0, smem_limit());
-  const size_t sm = (size_t)W * per_line;
+  const int cs = (int)sizeof(C), rin = a.min.rows();
+  auto bytes = [&](int w) {
+    return (size_t)w * ((size_t)3 * staged_rows(rin, w, cs) + axis_ld(N, w, cs)) * sizeof(C);
+  };
+  const size_t lim = smem_limit();
+  int W = 256 / G;
+  while (W > 2 && bytes(W) > lim) W >>= 1;
+  const size_t sm = bytes(W);
   k_axis_curl6<Real, N><<<(unsigned)((a.nlines + W - 1) / W), W * G, sm, s>>>(a);
   return (int)cudaGetLastError();
 }
