@@ -478,6 +478,104 @@ __device__ __forceinline__ void fwd_line_regs(C* buf, int g, const C* __restrict
   }
 }
 
+// ---------------------------------------------------------------------------
+// L independent lines transformed together (line l in buf + l*ldb): every
+// pass loads all L lines, applies each twiddle factor to all of them and
+// stores all of them, so the L dependency chains interleave and one twiddle
+// load serves L lines.  Forward sign; x[l][m] is position g + G*m.
+// ---------------------------------------------------------------------------
+template <int R, int N, int Ns, int L, typename C>
+__device__ __forceinline__ void stockham_pass_fL(C* buf, int ldb, int g, const C* __restrict__ tw) {
+  constexpr int E = 16, G = N / E, NB = E / R, NR = N / R;
+  C v[L][E];
+#pragma unroll
+  for (int q = 0; q < NB; ++q)
+#pragma unroll
+    for (int l = 0; l < L; ++l) load_r<R, NR>(buf + l * ldb, g + G * q, padq<G>(g, q), &v[l][q * R]);
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const int j = g + G * q;
+    const int k = j & (Ns - 1);
+    const C* t = tw + k;
+#pragma unroll
+    for (int r = 1; r < R; ++r) {
+      const C w = t[r * Ns];
+#pragma unroll
+      for (int l = 0; l < L; ++l) v[l][q * R + r] = cmul(v[l][q * R + r], w);
+    }
+#pragma unroll
+    for (int l = 0; l < L; ++l) dftR<R, -1>(&v[l][q * R]);
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const int j = g + G * q;
+    const int k = j & (Ns - 1);
+#pragma unroll
+    for (int l = 0; l < L; ++l) store_r<R, Ns>(buf + l * ldb, (j - k) * R + k, &v[l][q * R]);
+  }
+  __syncwarp();
+}
+
+template <int R, int N, int Ns, int L, typename C>
+__device__ __forceinline__ void last_pass_fL(const C* buf, int ldb, int g, const C* __restrict__ tw, C (&x)[L][16]) {
+  constexpr int E = 16, G = N / E, NB = E / R, NR = N / R;
+  C v[L][E];
+#pragma unroll
+  for (int q = 0; q < NB; ++q)
+#pragma unroll
+    for (int l = 0; l < L; ++l) load_r<R, NR>(buf + l * ldb, g + G * q, padq<G>(g, q), &v[l][q * R]);
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const C* t = tw + (g + G * q);  // j < Ns in the last pass
+#pragma unroll
+    for (int r = 1; r < R; ++r) {
+      const C w = t[r * Ns];
+#pragma unroll
+      for (int l = 0; l < L; ++l) v[l][q * R + r] = cmul(v[l][q * R + r], w);
+    }
+#pragma unroll
+    for (int l = 0; l < L; ++l) dftR<R, -1>(&v[l][q * R]);
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q)
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+      for (int l = 0; l < L; ++l) x[l][q + r * NB] = v[l][q * R + r];
+}
+
+template <int N, int Ns, int L, typename C>
+__device__ __forceinline__ void fwd_passes_L(C* buf, int ldb, int g, const C* __restrict__ tw, int off,
+                                             C (&x)[L][16]) {
+  constexpr int R = (N / Ns) >= 16 ? 16 : N / Ns;
+  if constexpr (Ns * R == N) {
+    last_pass_fL<R, N, Ns, L>(buf, ldb, g, tw + off, x);
+  } else {
+    stockham_pass_fL<R, N, Ns, L>(buf, ldb, g, tw + off);
+    fwd_passes_L<N, Ns * R, L>(buf, ldb, g, tw, off + R * Ns, x);
+  }
+}
+
+// forward transforms of L lines of compile-time length N (16..512) held in
+// registers (x[l][m] = position g + G*m in and out); buf holds L lines of ldb
+template <int N, int L, typename C>
+__device__ __forceinline__ void fwd_lines_regs(C* buf, int ldb, int g, const C* __restrict__ tw, C (&x)[L][16]) {
+#pragma unroll
+  for (int l = 0; l < L; ++l) dft16<-1>(x[l]);
+  if constexpr (N > 16) {
+    __syncwarp();  // earlier readers of buf are done
+#pragma unroll
+    for (int l = 0; l < L; ++l) {
+      C* b = buf + l * ldb + 17 * g;  // padp(16 g + r) = 17 g + r
+#pragma unroll
+      for (int r = 0; r < 16; ++r) b[r] = x[l][r];
+    }
+    __syncwarp();
+    fwd_passes_L<N, 16, L>(buf, ldb, g, tw, 16, x);
+  }
+}
+
 // Ampere-style asynchronous global->shared copies (LDGSTS); the data does not
 // pass through registers, so a whole tile can be in flight per thread block.
 __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {

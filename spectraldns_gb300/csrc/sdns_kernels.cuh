@@ -401,15 +401,18 @@ __global__ void __launch_bounds__(64) k_zline_ns(ZArgs a) {
   }
 }
 
+// complex values of shared memory per warp of k_zline_ns_t: LPW staging
+// areas of 6 rows and LPW x 3 line buffers (kept even: 16-byte alignment)
 __host__ __device__ inline size_t znsr_per_warp(int LD, int Kzp, int LPW) {
-  const size_t n = (size_t)LPW * ((size_t)6 * Kzp + (size_t)LD);
+  const size_t n = (size_t)LPW * ((size_t)6 * Kzp + (size_t)3 * LD);
   return (n + 1) & ~(size_t)1;
 }
 
-// Same sweep with the line length fixed at compile time and a single
-// forward-transform body reused for all five transforms of a line (the
-// three inverse ones as conj(fwd(conj(x))), the pack folded into the first
-// radix pass, the unpack done with warp shuffles).
+// Same sweep with the line length fixed at compile time.  The three inverse
+// transforms of a line run together (conj(fwd(conj(.))), one batched body
+// of three interleaved chains sharing the twiddle loads), then u x w, then
+// the two forward transforms together; the pack is folded into the first
+// pass and the unpack done with warp shuffles.
 template <typename Real, int N>
 __global__ void __launch_bounds__(64, 4) k_zline_ns_t(ZArgs a) {
   constexpr int E = 16, G = N / E, LPW = 32 / G;
@@ -422,7 +425,7 @@ __global__ void __launch_bounds__(64, 4) k_zline_ns_t(ZArgs a) {
   const int Kzp = a.Kzp, Kz = a.Kz;
   C* base = sm + (size_t)warp * znsr_per_warp(LD, Kzp, LPW);
   C* stg = base + (size_t)sub * 6 * Kzp;
-  C* buf = base + (size_t)LPW * 6 * Kzp + (size_t)sub * LD;
+  C* buf = base + (size_t)LPW * 6 * Kzp + (size_t)sub * 3 * LD;
   const C* tw = reinterpret_cast<const C*>(a.tw);
   const long long fs = a.nlines * Kzp;
   const C* in = reinterpret_cast<const C*>(a.in);
@@ -449,8 +452,8 @@ __global__ void __launch_bounds__(64, 4) k_zline_ns_t(ZArgs a) {
     const bool valid = line < a.nlines;
     cp_wait_all();
     __syncwarp();
-    C U0[E], U1[E], U2[E], X[E];
-#pragma unroll 1
+    C U[3][E];
+#pragma unroll
     for (int p = 0; p < 3; ++p) {
       const C* ra = stg + (2 * p) * Kzp;
       const C* rb = stg + (2 * p + 1) * Kzp;
@@ -468,37 +471,27 @@ __global__ void __launch_bounds__(64, 4) k_zline_ns_t(ZArgs a) {
             v = mk<C>(A.x + B.y, B.x - A.y);
           }
         }
-        X[m] = cconj(v);  // inverse = conj(fwd(conj(.)))
-      }
-      fwd_line_regs<N>(buf, g, tw, X);
-      if (p == 0) {
-#pragma unroll
-        for (int m = 0; m < E; ++m) U0[m] = cconj(X[m]);
-      } else if (p == 1) {
-#pragma unroll
-        for (int m = 0; m < E; ++m) U1[m] = cconj(X[m]);
-      } else {
-#pragma unroll
-        for (int m = 0; m < E; ++m) U2[m] = cconj(X[m]);
+        U[p][m] = cconj(v);  // inverse = conj(fwd(conj(.)))
       }
     }
+    fwd_lines_regs<N, 3>(buf, LD, g, tw, U);
     __syncwarp();
     stage(line + wstride);
-    // u x w in registers; U0 = (ux, uy), U1 = (uz, wx), U2 = (wy, wz)
-    C Z[E];
+    // u x w in registers; conj(U0) = (ux, uy), conj(U1) = (uz, wx), conj(U2) = (wy, wz)
+    C X[2][E];
 #pragma unroll
     for (int m = 0; m < E; ++m) {
-      const Real u0 = U0[m].x, u1 = U0[m].y, u2 = U1[m].x, w0 = U1[m].y, w1 = U2[m].x, w2 = U2[m].y;
+      const Real u0 = U[0][m].x, u1 = -U[0][m].y, u2 = U[1][m].x, w0 = -U[1][m].y, w1 = U[2][m].x,
+                 w2 = -U[2][m].y;
       if (a.cfl_rate && valid) rmax = fmax(rmax, fabs(u0) * idx0 + fabs(u1) * idx1 + fabs(u2) * idx2);
-      X[m] = mk<C>(u1 * w2 - u2 * w1, u2 * w0 - u0 * w2);
-      Z[m] = mk<C>(u0 * w1 - u1 * w0, (Real)0);
+      X[0][m] = mk<C>(u1 * w2 - u2 * w1, u2 * w0 - u0 * w2);
+      X[1][m] = mk<C>(u0 * w1 - u1 * w0, (Real)0);
     }
-    fwd_line_regs<N>(buf, g, tw, X);
-    fwd_line_regs<N>(buf, g, tw, Z);
+    fwd_lines_regs<N, 2>(buf, LD, g, tw, X);
     const long long lo = line * Kzp;
 #pragma unroll
     for (int m = 0; m < E; ++m) {
-      const C snd = (g == 0) ? X[(E - m) & (E - 1)] : X[E - 1 - m];
+      const C snd = (g == 0) ? X[0][(E - m) & (E - 1)] : X[0][E - 1 - m];
       C mir;
       mir.x = __shfl_sync(0xffffffffu, snd.x, src_lane);
       mir.y = __shfl_sync(0xffffffffu, snd.y, src_lane);
@@ -506,10 +499,10 @@ __global__ void __launch_bounds__(64, 4) k_zline_ns_t(ZArgs a) {
       if (valid && kz < Kzp) {
         C oa = czero<C>(), ob = czero<C>(), oc = czero<C>();
         if (kz < Kz) {
-          const C Xm = X[m];
+          const C Xm = X[0][m];
           oa = mk<C>((Real)0.5 * (Xm.x + mir.x), (Real)0.5 * (Xm.y - mir.y));
           ob = mk<C>((Real)0.5 * (Xm.y + mir.y), (Real)0.5 * (mir.x - Xm.x));
-          oc = Z[m];
+          oc = X[1][m];
         }
         out[lo + kz] = oa;
         out[fs + lo + kz] = ob;
