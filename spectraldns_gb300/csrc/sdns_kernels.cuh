@@ -436,11 +436,10 @@ __global__ void __launch_bounds__(64, 4) k_zline_ns_t(ZArgs a) {
   constexpr int VB = 16 / (int)sizeof(C);
   auto stage = [&](long long ln) {
     if (ln < a.nlines) {
-      const int nchunk = 6 * Kzp / VB;
-      for (int q = g; q < nchunk; q += G) {
-        const int f = (q * VB) / Kzp, k = q * VB - f * Kzp;
-        cp_async16(stg + f * Kzp + k, in + f * fs + ln * Kzp + k);
-      }
+      const C* src = in + ln * Kzp;
+#pragma unroll
+      for (int f = 0; f < 6; ++f)
+        for (int k = g * VB; k < Kzp; k += G * VB) cp_async16(stg + f * Kzp + k, src + f * fs + k);
     }
     cp_commit();
   };
@@ -491,6 +490,7 @@ __global__ void __launch_bounds__(64, 4) k_zline_ns_t(ZArgs a) {
     const long long lo = line * Kzp;
 #pragma unroll
     for (int m = 0; m < E; ++m) {
+      if (G * m >= Kzp) break;  // no lane stores from here on (warp-uniform)
       const C snd = (g == 0) ? X[0][(E - m) & (E - 1)] : X[0][E - 1 - m];
       C mir;
       mir.x = __shfl_sync(0xffffffffu, snd.x, src_lane);
