@@ -331,6 +331,25 @@ __device__ __forceinline__ void first16_c(C* buf, int g, Loader& ld) {
   __syncwarp();
 }
 
+// first radix-16 pass reading the line from `buf` itself (in place)
+template <int E, int S, int N, typename C>
+__device__ __forceinline__ void first16_buf(C* buf, int g) {
+  constexpr int R = 16, NB = E / R, NR = N / R, G = N / E;
+  C v[E];
+#pragma unroll
+  for (int q = 0; q < NB; ++q) load_r<R, NR>(buf, g + G * q, padq<G>(g, q), &v[q * R]);
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < NB; ++q) dftR<R, S>(&v[q * R]);
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    C* b = buf + 17 * (g + G * q);
+#pragma unroll
+    for (int r = 0; r < R; ++r) b[r] = v[q * R + r];
+  }
+  __syncwarp();
+}
+
 // Same transform with the line length N fixed at compile time: the pass
 // sequence, the strides and the twiddle offsets are constants, so the index
 // arithmetic of every pass folds into immediate offsets.
@@ -345,6 +364,12 @@ __device__ __forceinline__ void passes_t(C* buf, int g, const C* __restrict__ tw
 template <int N, int E, int S, typename C, typename Loader>
 __device__ __forceinline__ void line_fft_ld_t(C* buf, int g, const C* __restrict__ tw, Loader& ld) {
   first16_c<E, S, N>(buf, g, ld);
+  passes_t<N, E, S, 16>(buf, g, tw, 16);
+}
+// in-place transform of a line held in natural order in `buf`
+template <int N, int E, int S, typename C>
+__device__ __forceinline__ void line_fft_t(C* buf, int g, const C* __restrict__ tw) {
+  first16_buf<E, S, N>(buf, g);
   passes_t<N, E, S, 16>(buf, g, tw, 16);
 }
 

@@ -77,6 +77,9 @@ __global__ void __launch_bounds__(256, 3) k_axis_p(AxisArgs a) {
   const C* in = reinterpret_cast<const C*>(a.in);
   const C* tw = reinterpret_cast<const C*>(a.tw);
   const Real sc = (Real)a.scale;
+  // rows are staged at their line positions; the positions between the kept
+  // rows of a pruned input (kc < p < N - kc) are written with zeros
+  const int kcin = a.min.kc, shift = N - rin;
   auto issue = [&](unsigned f, unsigned tile, C* dst) {
     const unsigned l = tile * W + wc;
     if (l < nlines) {
@@ -84,7 +87,12 @@ __global__ void __launch_bounds__(256, 3) k_axis_p(AxisArgs a) {
       const C* src = in + (long long)f * a.in_fs + (long long)slab * a.in_ss + (l - slab * B) + (long long)r0 * a.in_rs;
       const long long step = (long long)G * a.in_rs;
       C* d = dst + wc * LD;
-      for (int r = r0; r < rin; r += G, src += step) cp_async<sizeof(C)>(d + padp(r), src);
+      if (kcin >= 0) {
+        for (int r = r0; r < rin; r += G, src += step) cp_async<sizeof(C)>(d + padp(r <= kcin ? r : r + shift), src);
+        for (int p = kcin + 1 + r0; p < N - kcin; p += G) d[padp(p)] = czero<C>();
+      } else {
+        for (int r = r0; r < rin; r += G, src += step) cp_async<sizeof(C)>(d + padp(r), src);
+      }
     }
     cp_commit();
   };
@@ -104,19 +112,7 @@ __global__ void __launch_bounds__(256, 3) k_axis_p(AxisArgs a) {
       cp_wait_all();
     }
     __syncthreads();
-    {
-      C* line = cur + wl * LD;
-      const RowMap mi = a.min;
-      auto ld = [&](int p) -> C {
-        int r = p;
-        if (mi.kc >= 0) {
-          if (p > mi.kc && p < N - mi.kc) return czero<C>();
-          if (p > mi.kc) r = p - N + 2 * mi.kc + 1;
-        }
-        return line[padp(r)];
-      };
-      line_fft_ld_t<N, E, S>(line, g, tw, ld);
-    }
+    line_fft_t<N, E, S>(cur + wl * LD, g, tw);
     __syncthreads();
     {
       C* out = reinterpret_cast<C*>(a.out) + (long long)f * a.out_fs;
