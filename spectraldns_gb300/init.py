@@ -82,9 +82,13 @@ def isotropic_field(N, L=(2 * np.pi,) * 3, k0=4.0, energy=0.5, seed=0, dealias="
     pl = uc[:, :, :, 0]
     uc[:, :, :, 0] = 0.5 * (pl + np.conj(pl[:, r0][:, :, r1]))
     uc[:, 0, 0, 0] = 0
-    w = np.full(len(j2), 2.0)
-    w[0] = 1.0
-    e = 0.5 * float(np.sum((np.abs(uc.astype(np.complex128)) ** 2) * w[None, None, None, :]))
+    # energy with the Hermitian weights (kz = 0 once, kz > 0 twice), summed in FP64
+    e = 0.0
+    for i in range(3):
+        a2 = uc[i].real ** 2 + uc[i].imag ** 2
+        e += 2.0 * float(np.sum(a2, dtype=np.float64)) - float(np.sum(a2[..., 0], dtype=np.float64))
+    del a2
+    e *= 0.5
     uc *= np.float32(math.sqrt(energy / e)) if e > 0 else 0
     out = np.zeros((3, n0, n1, n2 // 2 + 1), dtype=dtype)
     out[:, p0[:, None], p1[None, :], :kc[2] + 1] = uc

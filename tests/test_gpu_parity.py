@@ -22,8 +22,12 @@ def ctx(N, L, prec, **kw):
     return Context(N, L, nu=kw.pop("nu", 0.000625), precision=prec, **kw)
 
 
+# 1024-point axes (the E = 32 line kernels of the 1024^3 case) in each direction
+LONG = [((16, 16, 1024), (2 * np.pi,) * 3), ((1024, 16, 16), (2 * np.pi,) * 3), ((16, 1024, 16), (2 * np.pi,) * 3)]
+
+
 @pytest.mark.parametrize("prec", ["double", "single"])
-@pytest.mark.parametrize("N,L", GRIDS + [((128, 128, 128), (2 * np.pi,) * 3), ((256, 16, 32), (2 * np.pi,) * 3)])
+@pytest.mark.parametrize("N,L", GRIDS + [((128, 128, 128), (2 * np.pi,) * 3), ((256, 16, 32), (2 * np.pi,) * 3)] + LONG)
 def test_transforms(built_lib, N, L, prec):
     g = Grid(N, L)
     c = ctx(N, L, prec)
@@ -41,7 +45,7 @@ def test_transforms(built_lib, N, L, prec):
 
 @pytest.mark.parametrize("prec", ["double", "single"])
 @pytest.mark.parametrize("N,L", GRIDS + [((16, 16, 512), (2 * np.pi,) * 3), ((16, 32, 256), (2 * np.pi,) * 3),
-                                          ((128, 16, 128), (2 * np.pi,) * 3)])
+                                          ((128, 16, 128), (2 * np.pi,) * 3)] + LONG)
 def test_compute_rhs(built_lib, N, L, prec):
     g = Grid(N, L)
     uh = random_state(g, seed=3)
@@ -65,7 +69,7 @@ def test_compute_rhs_outside_modes(built_lib):
 
 
 @pytest.mark.parametrize("prec", ["double", "single"])
-@pytest.mark.parametrize("N,L", GRIDS[:3])
+@pytest.mark.parametrize("N,L", GRIDS[:3] + LONG[:2])
 def test_rk4_random(built_lib, N, L, prec):
     g = Grid(N, L, nu=0.01)
     uh = random_state(g, seed=5)
