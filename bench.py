@@ -51,6 +51,9 @@ def parse():
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-les", action="store_true", help="skip the closure-LES timing")
+    p.add_argument("--no-1024", action="store_true", help="skip the 1024^3 decaying-turbulence timing")
+    p.add_argument("--tg256", action="store_true",
+                   help="only run the 256^3 Taylor-Green FP32-vs-FP64 comparison (1000 steps) and print it")
     return p.parse_args()
 
 
@@ -280,12 +283,85 @@ def run_ours(args):
 
     if not args.no_les and n >= 64:
         out["les"] = les_measure(dev, n, dns_s_per_sim_time)
+    if not args.no_1024 and n == 512:
+        out["decaying_1024"] = decay_1024(dev, ws)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_sample(512 if n >= 512 else n)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def tg256(dev, steps=1000, n=256):
+    """Taylor-Green at 256^3, nu = 0.000625, dt = 0.005, 1000 RK4 steps in FP32 and in FP64 on the
+    GPU, with energy and dissipation (FP64 reductions) every step; the FP64 run is pinned to the
+    float64 oracle by the GPU tests.  Reports the largest relative FP32-FP64 differences and
+    both runs' steps/s."""
+    from spectraldns_gb300.gpu import Context
+    from spectraldns_gb300.init import taylor_green
+    N = (n,) * 3
+    nu, dt = 0.000625, 0.005
+    res = {"workload": "Taylor-Green %d^3, nu=0.000625, dt=0.005, %d RK4 steps, FP32 vs FP64" % (n, steps)}
+    series = {}
+    for prec in ("double", "single"):
+        c = Context(N, nu=nu, precision=prec, device=dev)
+        u0 = taylor_green(N)
+        c.set_state(c.forward(u0.astype(c.real)))
+        E, D = [], []
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            d = c.diagnostics()
+            E.append(d["energy"])
+            D.append(d["dissipation"])
+            c.rk4(dt, 1)
+        d = c.diagnostics()
+        E.append(d["energy"])
+        D.append(d["dissipation"])
+        wall = time.perf_counter() - t0
+        series[prec] = (np.array(E), np.array(D))
+        res[prec] = {"steps_per_s_with_diagnostics": steps / wall, "final_energy": E[-1], "final_dissipation": D[-1],
+                     "time": d["time"]}
+        c.close()
+    (E64, D64), (E32, D32) = series["double"], series["single"]
+    res["max_rel_diff_energy"] = float(np.max(np.abs(E32 - E64) / E64))
+    res["max_rel_diff_dissipation"] = float(np.max(np.abs(D32 - D64) / D64))
+    res["rel_diff_energy_step100"] = float(abs(E32[100] - E64[100]) / E64[100])
+    res["energy_every_100"] = [float(x) for x in E64[::100]]
+    res["dissipation_every_100"] = [float(x) for x in D64[::100]]
+    return res
+
+
+def decay_1024(dev, ws, steps=5):
+    """Decaying isotropic turbulence at 1024^3 FP32 (k0 = 6 spectrum, no forcing, nu = 4e-4,
+    RK4 at CFL 0.5) with FP64 energy and dissipation reductions: steps/s over `steps` steps."""
+    import torch
+    from spectraldns_gb300.gpu import Context
+    from spectraldns_gb300.init import isotropic_field
+    N = (1024,) * 3
+    uh = isotropic_field(N, k0=6.0, energy=0.5, seed=0, dtype=np.complex64)
+    c = Context(N, nu=4e-4, precision="single", device=dev)
+    c.set_cfl(CFL)
+    c.set_state(uh)
+    del uh
+    c.rk4(0.0, 2)
+    c.synchronize()
+    st = torch.cuda.ExternalStream(c.stream_handle(), device=torch.device("cuda", dev))
+    a0 = torch.cuda.Event(enable_timing=True)
+    a1 = torch.cuda.Event(enable_timing=True)
+    a0.record(st)
+    c.rk4(0.0, steps)
+    a1.record(st)
+    torch.cuda.synchronize(dev)
+    ms = a0.elapsed_time(a1)
+    d = c.diagnostics()
+    res = {"value": ws * steps / (ms / 1e3), "unit": "steps/s", "steps": steps, "warmup": 2,
+           "ms_per_step": ms / steps, "grid": list(N), "dtype": "f32", "hbm_bytes": c.memory_bytes(),
+           "energy": d["energy"], "dissipation": d["dissipation"], "time": d["time"],
+           "workload": "decaying isotropic turbulence 1024^3 FP32 (seeded k^4 exp(-2(k/6)^2), E=0.5, "
+                       "nu=4e-4, no forcing, RK4 CFL 0.5, FP64 reductions)"}
+    c.close()
+    return res
 
 
 def les_measure(dev, n_dns, dns_s_per_sim_time, ratio=8, steps=30):
@@ -299,7 +375,7 @@ def les_measure(dev, n_dns, dns_s_per_sim_time, ratio=8, steps=30):
     n = (nc,) * 3
     model = os.path.join(ROOT, "spectraldns_gb300", "data", "closure_%d.npz" % nc)
     if os.path.exists(model):
-        net, nm = L.load_model(model, n, device=dev)
+        net, nm, scale = L.load_model(model, n, device=dev)
         trained = True
     else:
         net = L.ClosureNet(n, device=dev)
@@ -307,7 +383,8 @@ def les_measure(dev, n_dns, dns_s_per_sim_time, ratio=8, steps=30):
         nm = {"fmu": torch.zeros(9, device=d), "fisd": torch.ones(9, device=d), "tmu": torch.zeros(6, device=d),
               "tsd": torch.full((6,), 1e-3, device=d)}
         trained = False
-    les = L.LES(n, net, nm, device=dev)
+        scale = 1.0
+    les = L.LES(n, net, nm, device=dev, scale=scale)
     les.ctx.set_state(isotropic_field(n, k0=4.0, energy=0.5, seed=0, dtype=np.complex64))
     for _ in range(3):
         les.step()
@@ -328,7 +405,8 @@ def les_measure(dev, n_dns, dns_s_per_sim_time, ratio=8, steps=30):
         with open(os.path.join(ROOT, "profiles", "les_closure_512to64.json")) as f:
             ex = json.load(f)
         ev = ex["evaluation"]
-        out["spectrum_err_k<=20"] = {"closure_final": ev["closure"]["max_err_k<=20_final"],
+        out["spectrum_err_k<=20"] = {"closure_scale": ev["closure"].get("scale", 1.0),
+                                     "closure_final": ev["closure"]["max_err_k<=20_final"],
                                      "closure_mean": ev["closure"]["max_err_k<=20_mean"],
                                      "no_closure_final": ev["no_closure"]["max_err_k<=20_final"],
                                      "no_closure_mean": ev["no_closure"]["max_err_k<=20_mean"],
@@ -404,7 +482,9 @@ def run_reference(args):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.tg256:
+        print(json.dumps(tg256(int(os.environ.get("LOCAL_RANK", "0")))), flush=True)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

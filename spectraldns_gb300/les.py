@@ -230,7 +230,8 @@ def harvest(n_dns=512, ratio=8, steps=2000, every=10, seed=0, device=0, log=prin
 class LES:
     """Coarse solver with an optional learned closure."""
 
-    def __init__(self, n, net: ClosureNet | None, norms=None, device=0):
+    def __init__(self, n, net: ClosureNet | None, norms=None, device=0, scale=1.0):
+        self.scale = float(scale)  # amplitude of the subgrid force (calibrated a posteriori)
         self.ctx = Context(n, nu=NU, precision="single", device=device)
         self.ctx.set_forcing(EPS, KF)
         self.ctx.set_cfl(CFL)
@@ -245,7 +246,8 @@ class LES:
         self.L = _lib.lib()
 
     def set_velocity_phys(self, ubar):
-        self.ctx.set_state(self.ctx.forward(ubar))
+        """Start from a filtered velocity, truncated to the modes the LES keeps (2/3 rule)."""
+        self.ctx.set_state(self.ctx.forward(ubar) * dealias_mask(self.ctx))
 
     def closure_source(self):
         nm = self.norms
@@ -258,7 +260,7 @@ class LES:
         self.ctx.forward(self.tau[0:3], out=self.tauhat[0:3])
         self.ctx.forward(self.tau[3:6], out=self.tauhat[3:6])
         check(self.L.sdns_les_sgs_force(_p(self.tauhat), _p(self.force), _lib.SDNS_SINGLE, _ivec(self.ctx.N),
-                                        _dvec(self.ctx.L), 1.0, _stream()))
+                                        _dvec(self.ctx.L), self.scale, _stream()))
         torch.cuda.synchronize()
         self.ctx.set_source(self.force)
 
@@ -281,17 +283,40 @@ def normalisers(feat_all, tau_all):
             "tsd": tsd.float().contiguous()}
 
 
+def dealias_mask(ctx: Context):
+    """2/3-rule mask of the full spectral array of a coarse context (the modes the LES keeps)."""
+    from .init import dealias_cutoff
+    d = torch.device("cuda", ctx.device)
+    n0, n1, n2 = ctx.N
+    kc = [dealias_cutoff(n) for n in ctx.N]
+    k0 = torch.fft.fftfreq(n0, 1.0 / n0).to(d).abs()
+    k1 = torch.fft.fftfreq(n1, 1.0 / n1).to(d).abs()
+    k2 = torch.arange(n2 // 2 + 1, device=d, dtype=torch.float32)
+    return (k0[:, None, None] <= kc[0]) & (k1[None, :, None] <= kc[1]) & (k2[None, None, :] <= kc[2])
+
+
 def make_training_set(data, ctx64, train_idx):
-    """Gradient features (bf16, channels last) and normalised targets of the training snapshots."""
+    """Gradient features (bf16, channels last) and normalised targets of the training snapshots.
+
+    The LES holds only the 2/3-rule modes of the filtered field, so the features are the
+    gradients of the truncated filtered velocity T(ubar), and the target stress adds to the
+    box-filter stress the stress of the truncated filtered modes themselves:
+    tau_ij + ubar_i ubar_j - T(ubar)_i T(ubar)_j."""
     feat = Features(ctx64)
     dev = data["ubar"].device
     nc = ctx64.N
     P = int(np.prod(nc))
+    mask = dealias_mask(ctx64)
+    pairs = [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]
     G = torch.empty((len(train_idx), 9, P), dtype=torch.float32, device=dev)
+    T = torch.empty((len(train_idx), P, 6), dtype=torch.float32, device=dev)
     for a, i in enumerate(train_idx):
-        uh = ctx64.forward(data["ubar"][i])
+        ub = data["ubar"][i]
+        uh = ctx64.forward(ub) * mask
+        ut = ctx64.backward(uh)
         G[a] = feat.gradients(uh).reshape(9, P)
-    T = data["tau"][train_idx]
+        tr = torch.stack([(ub[p] * ub[q] - ut[p] * ut[q]).reshape(P) for p, q in pairs], dim=1)
+        T[a] = data["tau"][i] + tr
     nm = normalisers(G, T)
     X = torch.empty((len(train_idx), P, CPAD_IN), dtype=torch.bfloat16, device=dev)
     for a in range(len(train_idx)):
@@ -300,14 +325,19 @@ def make_training_set(data, ctx64, train_idx):
     return X, Tn, nm
 
 
-def train(net: ClosureNet, X, Tn, iters=1500, log=print, seed=0):
+def train(net: ClosureNet, X, Tn, iters=1500, log=print, seed=0, cosine=True):
+    """Adam on random training snapshots; the learning rate decays from net.lr to 1% of it
+    along a cosine when `cosine` is set."""
     rng = np.random.default_rng(seed)
+    lr0 = net.lr
     L = _lib.lib()
     loss = torch.zeros(1, dtype=torch.float64, device=net.dev)
     grad = torch.empty((net.P, CPAD_OUT), dtype=torch.float32, device=net.dev)
     hist = []
     t0 = time.time()
     for it in range(iters):
+        if cosine:
+            net.lr = lr0 * (0.01 + 0.99 * 0.5 * (1.0 + math.cos(math.pi * it / max(iters - 1, 1))))
         i = int(rng.integers(0, X.shape[0]))
         y = net.forward(X[i])
         loss.zero_()
@@ -319,6 +349,7 @@ def train(net: ClosureNet, X, Tn, iters=1500, log=print, seed=0):
             if log and it % 250 == 0:
                 log("train it %d loss %.4f (%.1f s)" % (it, hist[-1][1], time.time() - t0))
     torch.cuda.synchronize()
+    net.lr = lr0
     return hist, time.time() - t0
 
 
@@ -329,48 +360,83 @@ def spectrum_error(E, Eref, kmax=20):
     return float(np.max(np.abs(E[idx] - Eref[idx]) / np.maximum(Eref[idx], 1e-300)))
 
 
-def evaluate(data, net, nm, start, nc, device=0, log=print):
-    """Run the LES with and without the closure from filtered-DNS snapshot `start` and compare spectra."""
+def spectrum_errors_k(E, Eref, kmax=20):
+    kmax = min(kmax, len(E) - 1)
+    idx = np.arange(kmax)
+    return (np.abs(E[idx] - Eref[idx]) / np.maximum(Eref[idx], 1e-300)).tolist()
+
+
+def run_les(data, net, nm, start, stop, nc, scale=1.0, device=0, scratch=None):
+    """LES from filtered-DNS snapshot `start` to snapshot `stop - 1`; the spectrum error against the
+    filtered DNS at every snapshot in between."""
     n = (nc,) * 3
     times = data["times"]
-    scratch = Context(n, nu=NU, precision="single", device=device)
-    res = {}
-    for name, use in (("closure", True), ("no_closure", False)):
-        les = LES(n, net if use else None, nm, device=device)
-        les.set_velocity_phys(data["ubar"][start])
-        les.ctx.set_time(times[start])
-        errs = []
-        gpu_s = 0.0
-        nsteps = 0
-        ok = True
-        for j in range(start + 1, len(times)):
-            while les.time() < times[j] - 1e-12:
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                les.step()
-                les.ctx.synchronize()
-                gpu_s += time.perf_counter() - t0
-                nsteps += 1
-            E = les.ctx.spectrum()
-            if not np.all(np.isfinite(E)):
-                ok = False
-                break
-            Eref = spectrum_of(scratch, scratch.forward(data["ubar"][j]))
-            errs.append(spectrum_error(E, Eref))
-        les_time = les.time() - times[start]
-        res[name] = {"max_err_k<=20_final": errs[-1] if errs else float("nan"),
-                     "max_err_k<=20_mean": float(np.mean(errs)) if errs else float("nan"),
-                     "finite": ok, "steps": nsteps, "sim_time": les_time, "wall_s": gpu_s,
-                     "s_per_sim_time": gpu_s / max(les_time, 1e-30)}
+    scratch = scratch or Context(n, nu=NU, precision="single", device=device)
+    les = LES(n, net, nm, device=device, scale=scale)
+    les.set_velocity_phys(data["ubar"][start])
+    les.ctx.set_time(times[start])
+    errs = []
+    gpu_s = 0.0
+    nsteps = 0
+    ok = True
+    E = Eref = None
+    for j in range(start + 1, stop):
+        while les.time() < times[j] - 1e-12:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            les.step()
+            les.ctx.synchronize()
+            gpu_s += time.perf_counter() - t0
+            nsteps += 1
+        E = les.ctx.spectrum()
+        if not np.all(np.isfinite(E)):
+            ok = False
+            break
+        Eref = spectrum_of(scratch, scratch.forward(data["ubar"][j]))
+        errs.append(spectrum_error(E, Eref))
+    les_time = les.time() - times[start]
+    les.ctx.close()
+    return {"max_err_k<=20_final": errs[-1] if (errs and ok) else float("inf"),
+            "max_err_k<=20_mean": float(np.mean(errs)) if (errs and ok) else float("inf"),
+            "finite": ok, "steps": nsteps, "sim_time": les_time, "wall_s": gpu_s,
+            "s_per_sim_time": gpu_s / max(les_time, 1e-30), "scale": scale,
+            "err_k_final": spectrum_errors_k(E, Eref) if (ok and E is not None) else None,
+            "spectrum_final": E[:22].tolist() if (ok and E is not None) else None,
+            "reference_final": Eref[:22].tolist() if Eref is not None else None}
+
+
+def calibrate(data, net, nm, start, stop, nc, scales, device=0, log=print):
+    """A-posteriori amplitude of the subgrid force: the scale with the lowest mean spectrum error of
+    the LES over training snapshots [start, stop)."""
+    scratch = Context((nc,) * 3, nu=NU, precision="single", device=device)
+    table = []
+    for sc in scales:
+        r = run_les(data, net, nm, start, stop, nc, scale=sc, device=device, scratch=scratch)
+        table.append((sc, r["max_err_k<=20_mean"], r["max_err_k<=20_final"]))
         if log:
-            log("%s: final err %.3f mean err %.3f steps %d" % (name, res[name]["max_err_k<=20_final"],
-                                                             res[name]["max_err_k<=20_mean"], nsteps))
-    E_les = les.ctx.spectrum()
-    res["spectra_final"] = {"les_no_closure": E_les[:24].tolist()}
+            log("calibrate scale %.2f: mean err %.3f final err %.3f" % table[-1])
+    best = min(table, key=lambda t: t[1])
+    return best[0], table
+
+
+def evaluate(data, net, nm, start, nc, device=0, log=print, scale=1.0):
+    """LES with the calibrated closure, the uncalibrated closure and no closure from filtered-DNS
+    snapshot `start` to the last one, compared with the filtered DNS."""
+    stop = len(data["times"])
+    res = {}
+    for name, use, sc in (("closure", True, scale), ("closure_scale1", True, 1.0), ("no_closure", False, 1.0)):
+        res[name] = run_les(data, net if use else None, nm, start, stop, nc, scale=sc, device=device)
+        if log:
+            log("%s (scale %.2f): final err %.3f mean err %.3f steps %d" % (
+                name, sc, res[name]["max_err_k<=20_final"], res[name]["max_err_k<=20_mean"], res[name]["steps"]))
     return res
 
 
-def run_experiment(out_json, n_dns=512, ratio=8, steps=2000, every=10, iters=1500, train_frac=0.75, log=print):
+SCALES = (0.5, 1.0, 1.5, 2.0, 2.5, 3.0, 4.0, 5.0, 6.0, 8.0)
+
+
+def run_experiment(out_json, n_dns=512, ratio=8, steps=2000, every=10, iters=3000, train_frac=0.75, log=print,
+                   scales=SCALES):
     data = harvest(n_dns, ratio, steps, every, log=log)
     nc = n_dns // ratio
     nsnap = data["ubar"].shape[0]
@@ -379,30 +445,36 @@ def run_experiment(out_json, n_dns=512, ratio=8, steps=2000, every=10, iters=150
     X, Tn, nm = make_training_set(data, ctx64, list(range(ntrain)))
     net = ClosureNet((nc,) * 3, seed=0)
     hist, train_s = train(net, X, Tn, iters=iters, log=log)
-    ev = evaluate(data, net, nm, ntrain, nc, log=log)
+    # amplitude calibration on the last 50 training snapshots (never on the evaluated ones)
+    c0 = max(0, ntrain - 50)
+    scale, table = calibrate(data, net, nm, c0, ntrain, nc, scales, log=log)
+    ev = evaluate(data, net, nm, ntrain, nc, log=log, scale=scale)
     dns_s_per_time = data["dns_gpu_ms"] / 1e3 / max(data["dns_time"], 1e-30)
     out = {"n_dns": n_dns, "n_les": nc, "ratio": ratio, "dns_steps": steps, "snapshots": nsnap, "train_snapshots": ntrain,
            "train_iters": iters, "train_loss_first": hist[0][1], "train_loss_last": hist[-1][1], "train_s": train_s,
+           "calibration": {"snapshots": [c0, ntrain], "scale": scale, "table": table},
            "dns_gpu_s_per_sim_time": dns_s_per_time, "evaluation": ev,
            "speedup_gpu_seconds": dns_s_per_time / ev["closure"]["s_per_sim_time"],
            "speedup_no_closure": dns_s_per_time / ev["no_closure"]["s_per_sim_time"]}
     with open(out_json, "w") as f:
         json.dump(out, f, indent=1)
-    save_model(os.path.splitext(out_json)[0] + "_model.npz", net, nm)
+    save_model(os.path.splitext(out_json)[0] + "_model.npz", net, nm, scale)
     return out
 
 
-def save_model(path, net, nm):
-    np.savez(path, w=net.state_dict()["w"], **{k: v.cpu().numpy() for k, v in nm.items()})
+def save_model(path, net, nm, scale=1.0):
+    np.savez(path, w=net.state_dict()["w"], scale=np.float64(scale), **{k: v.cpu().numpy() for k, v in nm.items()})
 
 
 def load_model(path, n, device=0):
+    """(net, normalisers, calibrated subgrid-force scale) of a saved closure."""
     d = np.load(path)
     net = ClosureNet(n, device=device)
     net.load(d["w"])
     dev = torch.device("cuda", device)
     nm = {k: torch.from_numpy(d[k]).to(dev) for k in ("fmu", "fisd", "tmu", "tsd")}
-    return net, nm
+    scale = float(d["scale"]) if "scale" in d.files else 1.0
+    return net, nm, scale
 
 
 if __name__ == "__main__":
@@ -413,7 +485,7 @@ if __name__ == "__main__":
     ap.add_argument("--ratio", type=int, default=8)
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--every", type=int, default=10)
-    ap.add_argument("--iters", type=int, default=1500)
+    ap.add_argument("--iters", type=int, default=3000)
     a = ap.parse_args()
     r = run_experiment(a.out, a.n, a.ratio, a.steps, a.every, a.iters, log=lambda s: print(s, flush=True))
     print(json.dumps({k: v for k, v in r.items() if k != "evaluation"}))
