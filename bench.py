@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-les", action="store_true", help="skip the closure-LES timing")
     p.add_argument("--no-1024", action="store_true", help="skip the 1024^3 decaying-turbulence timing")
+    p.add_argument("--grid", default=None,
+                   help="N0,N1,N2: run the workload on this (small, profiling) grid instead of --n cubed")
     p.add_argument("--tg256", action="store_true",
                    help="only run the 256^3 Taylor-Green FP32-vs-FP64 comparison (1000 steps) and print it")
     return p.parse_args()
@@ -127,20 +129,23 @@ class Clocks:
 # ---------------------------------------------------------------------------
 # algorithmic bytes per launch of each kernel class (FP32 state, FP64 RK4 accumulators)
 # ---------------------------------------------------------------------------
-def kernel_bytes(n, csz=8, acc=16):
+def kernel_bytes(N, csz=8, acc=16):
+    """Algorithmic HBM bytes per launch of each kernel class of one RK4 stage on grid N (an int
+    for a cubic grid): every input read once, every output written once."""
     from spectraldns_gb300.init import dealias_cutoff
-    kc = dealias_cutoff(n)
-    K = 2 * kc + 1
-    Kz = kc + 1
+    n0, n1, n2 = (N, N, N) if isinstance(N, int) else tuple(N)
+    K0 = 2 * dealias_cutoff(n0) + 1
+    K1 = 2 * dealias_cutoff(n1) + 1
+    Kz = dealias_cutoff(n2) + 1
     Kzp = (Kz + 7) // 8 * 8
-    comp = K * K * Kzp          # one compact component
-    a1 = n * K * Kzp            # one field after the first inverse axis
-    a2 = n * n * Kzp            # one field after the second inverse axis
+    comp = K0 * K1 * Kzp        # one compact component
+    a1 = n0 * K1 * Kzp          # one field after the first inverse axis
+    a2 = n0 * n1 * Kzp          # one field after the second inverse axis
     rk_state = comp * 3 * ((acc + csz + acc) + 2 * (csz + 3 * acc + csz) + (csz + 2 * acc + csz)) / 4.0
     return {
         "x_inv_curl": 3 * comp * csz + 6 * a1 * csz,
         "y_inv": 6 * a1 * csz + 6 * a2 * csz,
-        "z_c2r_cross_r2c": 6 * n * n * Kz * csz + 3 * a2 * csz,
+        "z_c2r_cross_r2c": 6 * n0 * n1 * Kz * csz + 3 * a2 * csz,
         "y_fwd": 3 * a2 * csz + 3 * a1 * csz,
         "x_fwd": 3 * a1 * csz + 3 * comp * csz,
         "rk_update": 3 * comp * csz + rk_state,
@@ -159,7 +164,7 @@ def run_ours(args):
         torch.cuda.set_device(local)
     dev = local
     n = args.n
-    N = (n, n, n)
+    N = tuple(int(x) for x in args.grid.split(",")) if args.grid else (n, n, n)
     uh0 = isotropic_field(N, k0=K0, energy=0.5, seed=0, dtype=np.complex64)
     ctx = Context(N, nu=NU, precision="single", device=dev)
     ctx.set_forcing(EPS, KF)
@@ -196,7 +201,7 @@ def run_ours(args):
     value = ws * args.steps / (ms_max / 1e3)
 
     # per-kernel roofline
-    kb = kernel_bytes(n)
+    kb = kernel_bytes(N)
     peak, peak_src = peaks()
     kernels = {}
     for i, name in enumerate(KERNEL_NAMES):
@@ -226,7 +231,7 @@ def run_ours(args):
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded spectrum, generated on the host; no dataset)",
-           "config": {"workload": WORKLOAD, "grid": [n, n, n], "precision": "single (FP32 transforms, FP64 RK4 "
+           "config": {"workload": WORKLOAD, "grid": list(N), "precision": "single (FP32 transforms, FP64 RK4 "
                       "accumulators and reductions)", "l2": "inputs larger than L2 (1.6 GB state), no flush",
                       "parallelism": "replicas" if ws > 1 else "single GPU",
                       "timing": "CUDA events on the solver stream; per-kernel events in the same region"},
@@ -406,6 +411,9 @@ def les_measure(dev, n_dns, dns_s_per_sim_time, ratio=8, steps=30):
             ex = json.load(f)
         ev = ex["evaluation"]
         out["spectrum_err_k<=20"] = {"closure_scale": ev["closure"].get("scale", 1.0),
+                                     "closure_time_avg_spectrum": ev["closure"].get("max_err_k<=20_time_avg_spectrum"),
+                                     "no_closure_time_avg_spectrum": ev["no_closure"].get(
+                                         "max_err_k<=20_time_avg_spectrum"),
                                      "closure_final": ev["closure"]["max_err_k<=20_final"],
                                      "closure_mean": ev["closure"]["max_err_k<=20_mean"],
                                      "no_closure_final": ev["no_closure"]["max_err_k<=20_final"],
