@@ -254,6 +254,27 @@ __device__ __forceinline__ void store_r(C* buf, int j, const C* v) {
   }
 }
 
+// Twiddles of a pass from few table loads (FP32: the loads, not the
+// arithmetic, are the scarce resource of the shared-memory-bound sweeps).
+// Radix 16: w^r for r = 1..15 from the loaded w^1, w^2, w^4, w^8, each product
+// at most three multiplications deep.
+template <typename C>
+__device__ __forceinline__ void powers16(const C* t, int Ns, C (&w)[16]) {
+  w[1] = t[Ns]; w[2] = t[2 * Ns]; w[4] = t[4 * Ns]; w[8] = t[8 * Ns];
+  w[3] = cmul(w[1], w[2]); w[5] = cmul(w[1], w[4]); w[6] = cmul(w[2], w[4]); w[7] = cmul(w[3], w[4]);
+#pragma unroll
+  for (int r = 9; r < 16; ++r) w[r] = cmul(w[r - 8], w[8]);
+}
+// exp(-2 pi i q/16) = (cos(pi q/8), -sin(pi q/8)), q = 0..7
+__device__ __forceinline__ constexpr double w16c(int q) {
+  return q == 0 ? 1.0 : q == 1 ? SDNS_C8 : q == 2 ? SDNS_R2 : q == 3 ? SDNS_S8 : q == 4 ? 0.0 : q == 5 ? -SDNS_S8
+       : q == 6 ? -SDNS_R2 : -SDNS_C8;
+}
+__device__ __forceinline__ constexpr double w16s(int q) {
+  return q == 0 ? 0.0 : q == 1 ? SDNS_S8 : q == 2 ? SDNS_R2 : q == 3 ? SDNS_C8 : q == 4 ? 1.0 : q == 5 ? SDNS_C8
+       : q == 6 ? SDNS_R2 : SDNS_S8;
+}
+
 template <int R, int E, int S, int N, int Ns, typename C>
 __device__ __forceinline__ void stockham_pass_c(C* buf, int g, const C* __restrict__ tw) {
   constexpr int G = N / E, NB = E / R, NR = N / R;
@@ -261,17 +282,34 @@ __device__ __forceinline__ void stockham_pass_c(C* buf, int g, const C* __restri
 #pragma unroll
   for (int q = 0; q < NB; ++q) load_r<R, NR>(buf, g + G * q, padq<G>(g, q), &v[q * R]);
   __syncwarp();
+  constexpr bool f32 = sizeof(C) == 8;
+  // last radix-2 pass of the compact sweeps: the twiddle of butterfly j = g + G q is
+  // W_N^g * exp(-2 pi i q/16) (G = N/16): one load per lane
+  constexpr bool tw_const = f32 && R == 2 && E == 16 && 2 * Ns == N && NB > 1;
+  C w0 = mk<C>(0, 0);
+  if constexpr (tw_const) w0 = tw[Ns + g];
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     const int j = g + G * q;
     const int k = j & (Ns - 1);
     if constexpr (Ns > 1) {
       const C* t = tw + k;
+      if constexpr (f32 && R == 16) {
+        C w[16];
+        powers16(t, Ns, w);
 #pragma unroll
-      for (int r = 1; r < R; ++r) {
-        C w = t[r * Ns];
+        for (int r = 1; r < R; ++r) v[q * R + r] = cmul(v[q * R + r], S > 0 ? cconj(w[r]) : w[r]);
+      } else if constexpr (tw_const) {
+        C w = mulc<-1>(w0, w16c(q), w16s(q));
         if (S > 0) w.y = -w.y;
-        v[q * R + r] = cmul(v[q * R + r], w);
+        v[q * R + 1] = cmul(v[q * R + 1], w);
+      } else {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          C w = t[r * Ns];
+          if (S > 0) w.y = -w.y;
+          v[q * R + r] = cmul(v[q * R + r], w);
+        }
       }
     }
     dftR<R, S>(&v[q * R]);
