@@ -346,8 +346,15 @@ __device__ __forceinline__ void last_pass_regs_c(const C* buf, int g, const C* _
     for (int r = 0; r < R; ++r) x[q + r * NB] = v[q * R + r];
 }
 
+// Pruned inverse transforms: with the 2/3 rule the kept input positions are
+// p <= kc and p >= N - kc, and kc < 6N/16, so the first pass's inputs
+// j + r*N/16 with r = 6..9 are zero for every j.  PR = true skips them (the
+// radix-16 butterfly then folds the zeros away).
+__host__ __device__ constexpr bool prunable(int n, int kc) { return kc >= 0 && kc < 6 * (n / 16); }
+__host__ __device__ constexpr bool pruned_r(int r) { return r >= 6 && r <= 9; }
+
 // first radix-16 pass fed by a loader; result written in natural order
-template <int E, int S, int N, typename C, typename Loader>
+template <int E, int S, int N, bool PR = false, typename C, typename Loader>
 __device__ __forceinline__ void first16_c(C* buf, int g, Loader& ld) {
   constexpr int R = 16, NB = E / R, NR = N / R, G = N / E;
   C v[E];
@@ -355,7 +362,7 @@ __device__ __forceinline__ void first16_c(C* buf, int g, Loader& ld) {
   for (int q = 0; q < NB; ++q) {
     const int j = g + G * q;
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[q * R + r] = ld(j + r * NR);
+    for (int r = 0; r < R; ++r) v[q * R + r] = (PR && pruned_r(r)) ? mk<C>(0, 0) : ld(j + r * NR);
   }
   __syncwarp();
 #pragma unroll
@@ -370,12 +377,26 @@ __device__ __forceinline__ void first16_c(C* buf, int g, Loader& ld) {
 }
 
 // first radix-16 pass reading the line from `buf` itself (in place)
-template <int E, int S, int N, typename C>
+template <int E, int S, int N, bool PR = false, typename C>
 __device__ __forceinline__ void first16_buf(C* buf, int g) {
   constexpr int R = 16, NB = E / R, NR = N / R, G = N / E;
   C v[E];
+  if constexpr (PR && NR % 16 == 0) {
 #pragma unroll
-  for (int q = 0; q < NB; ++q) load_r<R, NR>(buf, g + G * q, padq<G>(g, q), &v[q * R]);
+    for (int q = 0; q < NB; ++q) {
+      const C* b = buf + padq<G>(g, q);
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[q * R + r] = pruned_r(r) ? mk<C>(0, 0) : b[r * pstride<NR>()];
+    }
+  } else if constexpr (PR) {
+#pragma unroll
+    for (int q = 0; q < NB; ++q)
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[q * R + r] = pruned_r(r) ? mk<C>(0, 0) : buf[padp(g + G * q + r * NR)];
+  } else {
+#pragma unroll
+    for (int q = 0; q < NB; ++q) load_r<R, NR>(buf, g + G * q, padq<G>(g, q), &v[q * R]);
+  }
   __syncwarp();
 #pragma unroll
   for (int q = 0; q < NB; ++q) dftR<R, S>(&v[q * R]);
@@ -399,15 +420,15 @@ __device__ __forceinline__ void passes_t(C* buf, int g, const C* __restrict__ tw
     passes_t<N, E, S, Ns * R>(buf, g, tw, off + R * Ns);
   }
 }
-template <int N, int E, int S, typename C, typename Loader>
+template <int N, int E, int S, bool PR = false, typename C, typename Loader>
 __device__ __forceinline__ void line_fft_ld_t(C* buf, int g, const C* __restrict__ tw, Loader& ld) {
-  first16_c<E, S, N>(buf, g, ld);
+  first16_c<E, S, N, PR>(buf, g, ld);
   passes_t<N, E, S, 16>(buf, g, tw, 16);
 }
 // in-place transform of a line held in natural order in `buf`
-template <int N, int E, int S, typename C>
+template <int N, int E, int S, bool PR = false, typename C>
 __device__ __forceinline__ void line_fft_t(C* buf, int g, const C* __restrict__ tw) {
-  first16_buf<E, S, N>(buf, g);
+  first16_buf<E, S, N, PR>(buf, g);
   passes_t<N, E, S, 16>(buf, g, tw, 16);
 }
 

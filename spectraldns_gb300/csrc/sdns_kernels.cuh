@@ -80,6 +80,7 @@ __global__ void __launch_bounds__(256, 3) k_axis_p(AxisArgs a) {
   // rows are staged at their line positions; the positions between the kept
   // rows of a pruned input (kc < p < N - kc) are written with zeros
   const int kcin = a.min.kc, shift = N - rin;
+  const bool prune = prunable(N, kcin);
   auto issue = [&](unsigned f, unsigned tile, C* dst) {
     const unsigned l = tile * W + wc;
     if (l < nlines) {
@@ -89,7 +90,12 @@ __global__ void __launch_bounds__(256, 3) k_axis_p(AxisArgs a) {
       C* d = dst + wc * LD;
       if (kcin >= 0) {
         for (int r = r0; r < rin; r += G, src += step) cp_async<sizeof(C)>(d + padp(r <= kcin ? r : r + shift), src);
-        for (int p = kcin + 1 + r0; p < N - kcin; p += G) d[padp(p)] = czero<C>();
+        if (prune) {  // positions 6N/16 .. 10N/16-1 are never read (pruned first pass)
+          for (int p = kcin + 1 + r0; p < 6 * (N / 16); p += G) d[padp(p)] = czero<C>();
+          for (int p = 10 * (N / 16) + r0; p < N - kcin; p += G) d[padp(p)] = czero<C>();
+        } else {
+          for (int p = kcin + 1 + r0; p < N - kcin; p += G) d[padp(p)] = czero<C>();
+        }
       } else {
         for (int r = r0; r < rin; r += G, src += step) cp_async<sizeof(C)>(d + padp(r), src);
       }
@@ -112,7 +118,8 @@ __global__ void __launch_bounds__(256, 3) k_axis_p(AxisArgs a) {
       cp_wait_all();
     }
     __syncthreads();
-    line_fft_t<N, E, S>(cur + wl * LD, g, tw);
+    if (prune) line_fft_t<N, E, S, true>(cur + wl * LD, g, tw);
+    else line_fft_t<N, E, S, false>(cur + wl * LD, g, tw);
     __syncthreads();
     {
       C* out = reinterpret_cast<C*>(a.out) + (long long)f * a.out_fs;
@@ -242,7 +249,8 @@ __global__ void __launch_bounds__(256, 2) k_axis_curl6(AxisArgs a) {
       }
       return mk<C>(-t.y, t.x);
     };
-    line_fft_ld_t<N, E, 1>(line, g, tw, ld);
+    if (prunable(N, mi.kc)) line_fft_ld_t<N, E, 1, true>(line, g, tw, ld);
+    else line_fft_ld_t<N, E, 1, false>(line, g, tw, ld);
     __syncthreads();
     C* out = reinterpret_cast<C*>(a.out) + f * a.out_fs;
     if constexpr (sizeof(C) == 8) {
@@ -409,7 +417,7 @@ __host__ __device__ inline size_t znsr_per_warp(int LD, int Kzp, int LPW) {
 // of three interleaved chains sharing the twiddle loads), then u x w, then
 // the two forward transforms together; the pack is folded into the first
 // pass and the unpack done with warp shuffles.
-template <typename Real, int N>
+template <typename Real, int N, bool PR>
 __global__ void __launch_bounds__(64, 4) k_zline_ns_t(ZArgs a) {
   constexpr int E = 16, G = N / E, LPW = 32 / G;
   using C = typename cplx_of<Real>::type;
@@ -456,6 +464,10 @@ __global__ void __launch_bounds__(64, 4) k_zline_ns_t(ZArgs a) {
       for (int m = 0; m < E; ++m) {
         const int P = g + G * m;
         C v = czero<C>();
+        if (PR && pruned_r(m)) {  // kc < P < N - kc for every lane: zero (the first pass folds it away)
+          U[p][m] = v;
+          continue;
+        }
         if (valid) {
           if (P < Kz) {
             C A = ra[P], B = rb[P];
@@ -1094,14 +1106,14 @@ static int launch_z(const ZArgs& a, cudaStream_t s) {
   return (int)cudaGetLastError();
 }
 
-template <typename Real, int N>
+template <typename Real, int N, bool PR>
 static int launch_zns_t(const ZArgs& a, cudaStream_t s) {
   using C = typename cplx_of<Real>::type;
   constexpr int G = N / 16, LPW = 32 / G;
   const int warps = 2;
   if (a.Kzp % 8 != 0 || a.n != N) return (int)cudaErrorInvalidValue;
   const size_t sm = (size_t)warps * znsr_per_warp(line_ld(N), a.Kzp, LPW) * sizeof(C);
-  auto kern = k_zline_ns_t<Real, N>;
+  auto kern = k_zline_ns_t<Real, N, PR>;
   int dev = 0, nsm = 148, occ = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -1114,17 +1126,21 @@ static int launch_zns_t(const ZArgs& a, cudaStream_t s) {
   return (int)cudaGetLastError();
 }
 
-template <typename Real>
-int Kernels<Real>::zline_ns(const ZArgs& a, cudaStream_t s) {
+template <typename Real, bool PR>
+static int zns_n(const ZArgs& a, cudaStream_t s) {
   switch (a.n) {
-    case 16: return launch_zns_t<Real, 16>(a, s);
-    case 32: return launch_zns_t<Real, 32>(a, s);
-    case 64: return launch_zns_t<Real, 64>(a, s);
-    case 128: return launch_zns_t<Real, 128>(a, s);
-    case 256: return launch_zns_t<Real, 256>(a, s);
-    case 512: return launch_zns_t<Real, 512>(a, s);
+    case 16: return launch_zns_t<Real, 16, PR>(a, s);
+    case 32: return launch_zns_t<Real, 32, PR>(a, s);
+    case 64: return launch_zns_t<Real, 64, PR>(a, s);
+    case 128: return launch_zns_t<Real, 128, PR>(a, s);
+    case 256: return launch_zns_t<Real, 256, PR>(a, s);
+    case 512: return launch_zns_t<Real, 512, PR>(a, s);
     default: return launch_zns<Real, 32>(a, s);
   }
+}
+template <typename Real>
+int Kernels<Real>::zline_ns(const ZArgs& a, cudaStream_t s) {
+  return prunable(a.n, a.Kz - 1) ? zns_n<Real, true>(a, s) : zns_n<Real, false>(a, s);
 }
 template <typename Real>
 int Kernels<Real>::zline_c2r(const ZArgs& a, cudaStream_t s) {
@@ -1179,8 +1195,9 @@ int Kernels<Real>::smem_optin(int dev) {
   SDNS_OPT_N(16); SDNS_OPT_N(32); SDNS_OPT_N(64); SDNS_OPT_N(128); SDNS_OPT_N(256); SDNS_OPT_N(512); SDNS_OPT_N(1024);
 #undef SDNS_OPT_N
   SDNS_OPT((k_zline_ns<Real, 16>)); SDNS_OPT((k_zline_ns<Real, 32>));
-  SDNS_OPT((k_zline_ns_t<Real, 16>)); SDNS_OPT((k_zline_ns_t<Real, 32>)); SDNS_OPT((k_zline_ns_t<Real, 64>));
-  SDNS_OPT((k_zline_ns_t<Real, 128>)); SDNS_OPT((k_zline_ns_t<Real, 256>)); SDNS_OPT((k_zline_ns_t<Real, 512>));
+#define SDNS_OPT_Z(n) SDNS_OPT((k_zline_ns_t<Real, n, true>)); SDNS_OPT((k_zline_ns_t<Real, n, false>))
+  SDNS_OPT_Z(16); SDNS_OPT_Z(32); SDNS_OPT_Z(64); SDNS_OPT_Z(128); SDNS_OPT_Z(256); SDNS_OPT_Z(512);
+#undef SDNS_OPT_Z
   SDNS_OPT((k_zline<Real, 16, 1>)); SDNS_OPT((k_zline<Real, 16, 2>));
   SDNS_OPT((k_zline<Real, 32, 1>)); SDNS_OPT((k_zline<Real, 32, 2>));
   SDNS_OPT((k_axis_rk<Real, 16>)); SDNS_OPT((k_axis_rk<Real, 32>));
