@@ -896,13 +896,14 @@ int sdns_set_state(sdns_ctx* c, const void* u_hat, int where) {
   int hflag = 0;
   CK(cudaMemcpyAsync(&hflag, c->flag, 4, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
+  const bool was_high = c->high;
   c->high = hflag != 0;
   if (c->high) {
     if (!c->H && (e = dalloc(c, &c->H, 3 * c->nfull1 * (long long)c->csz))) return e;
     CK(cudaMemcpyAsync(c->H, c->stage, 3 * c->nfull1 * c->csz, cudaMemcpyDeviceToDevice, c->st));
   }
   c->has_state = true;
-  c->gkey = ~0ull;  // graph depends on `high`
+  if (c->high != was_high) c->gkey = ~0ull;  // the step graph depends on `high`
   return SDNS_OK;
 }
 
