@@ -244,6 +244,115 @@ __global__ void __launch_bounds__(256) k_conv3(const TIN* __restrict__ x, const 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Forward convolution on the tensor cores: an implicit GEMM per 8^3 brick,
+// D[point][o] = b[o] + sum_t sum_i X[point + d(t)][i] W[t][o][i], with BF16
+// mma.sync m16n8k16 and FP32 accumulation.  The brick's 10^3 halo (channels
+// last) and all 27 x CO rows of CI weights are staged in shared memory with
+// the 16-byte chunks of every row XOR-swizzled, so that the fragment loads of
+// 8 consecutive rows hit distinct banks.  Each warp owns 4 M-tiles of 16
+// points (two z-lines of 8) and all CO/8 N-tiles.
+// ---------------------------------------------------------------------------
+template <int CI> __device__ __forceinline__ int swz(int row) { return CI == 16 ? ((row >> 2) & 1) : ((row >> 1) & 3); }
+// byte offset of element k (even) of row `row` in a swizzled [rows][CI] BF16 array
+template <int CI> __device__ __forceinline__ int soff(int row, int k) {
+  return row * (CI * 2) + (((k >> 3) ^ swz<CI>(row)) << 4) + ((k & 7) << 1);
+}
+__device__ __forceinline__ uint32_t lds32(const unsigned char* p) { return *reinterpret_cast<const uint32_t*>(p); }
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+template <int CI, int CO> struct MmaSmem {
+  static constexpr size_t xbytes = (size_t)HB * HB * HB * CI * 2;
+  static constexpr size_t bytes = xbytes + (size_t)27 * CO * CI * 2;
+};
+
+template <int CI, int CO>
+__global__ void __launch_bounds__(256) k_conv3_mma(const bf16* __restrict__ x, const bf16* __restrict__ W,
+                                                   const float* __restrict__ bias, float* __restrict__ y,
+                                                   bf16* __restrict__ yact, int n0, int n1, int n2, int relu) {
+  static_assert(CI == 16 || CI == 32, "16 or 32 input channels");
+  static_assert(CO % 8 == 0, "output channels in multiples of 8");
+  constexpr int NCH = CI / 8, NT = CO / 8;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  unsigned char* sx = smraw;                              // [HB^3][CI] swizzled
+  unsigned char* sw = smraw + MmaSmem<CI, CO>::xbytes;    // [27*CO][CI] swizzled
+  const int nbx = n2 / BR, nby = n1 / BR;
+  const int bz = blockIdx.x % nbx, by = (blockIdx.x / nbx) % nby, bxx = blockIdx.x / (nbx * nby);
+  const int o0 = bxx * BR, o1 = by * BR, o2 = bz * BR;
+  for (int e = threadIdx.x; e < 27 * CO * NCH; e += blockDim.x) {
+    const int R = e / NCH, c = e % NCH;
+    *reinterpret_cast<uint4*>(sw + R * (CI * 2) + ((c ^ swz<CI>(R)) << 4)) = reinterpret_cast<const uint4*>(W)[e];
+  }
+  for (int e = threadIdx.x; e < HB * HB * HB * NCH; e += blockDim.x) {
+    const int h = e / NCH, c = e % NCH;
+    const int h2 = h % HB, h1 = (h / HB) % HB, h0 = h / (HB * HB);
+    const int g0 = wrap(o0 + h0 - 1, n0), g1 = wrap(o1 + h1 - 1, n1), g2 = wrap(o2 + h2 - 1, n2);
+    const uint4* src = reinterpret_cast<const uint4*>(x + (((long long)g0 * n1 + g1) * n2 + g2) * CI);
+    *reinterpret_cast<uint4*>(sx + h * (CI * 2) + ((c ^ swz<CI>(h)) << 4)) = src[c];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gq = lane >> 2, tq = lane & 3;
+  float acc[4][NT][4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[m][nt][q] = 0.f;
+#pragma unroll 1
+  for (int t = 0; t < 27; ++t) {
+    const int d0 = t / 9 - 1, d1 = (t / 3) % 3 - 1, d2 = t % 3 - 1;
+#pragma unroll
+    for (int kc = 0; kc < CI / 16; ++kc) {
+      uint32_t bfr[NT][2];
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) {
+        const int R = t * CO + nt * 8 + gq;
+        bfr[nt][0] = lds32(sw + soff<CI>(R, kc * 16 + 2 * tq));
+        bfr[nt][1] = lds32(sw + soff<CI>(R, kc * 16 + 8 + 2 * tq));
+      }
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const int mt = warp * 4 + m;
+        const int px = mt >> 2, py = 2 * (mt & 3);
+        const int h = ((px + 1 + d0) * HB + (py + 1 + d1)) * HB + (gq + 1 + d2);  // point (px, py, gq)
+        const int h8 = h + HB;                                                      // point (px, py + 1, gq)
+        uint32_t a[4];
+        a[0] = lds32(sx + soff<CI>(h, kc * 16 + 2 * tq));
+        a[1] = lds32(sx + soff<CI>(h8, kc * 16 + 2 * tq));
+        a[2] = lds32(sx + soff<CI>(h, kc * 16 + 8 + 2 * tq));
+        a[3] = lds32(sx + soff<CI>(h8, kc * 16 + 8 + 2 * tq));
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) mma_bf16(acc[m][nt], a, bfr[nt]);
+      }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const int mt = warp * 4 + m;
+    const int px = mt >> 2, py = 2 * (mt & 3);
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const long long p = ((long long)(o0 + px) * n1 + (o1 + py + half)) * n2 + (o2 + gq);
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) {
+        const int col = nt * 8 + 2 * tq;
+        const float v0 = acc[m][nt][2 * half] + (bias ? bias[col] : 0.f);
+        const float v1 = acc[m][nt][2 * half + 1] + (bias ? bias[col + 1] : 0.f);
+        *reinterpret_cast<float2*>(y + p * CO + col) = make_float2(v0, v1);
+        if (yact)
+          *reinterpret_cast<__nv_bfloat162*>(yact + p * CO + col) =
+              __floats2bfloat162_rn(relu ? fmaxf(v0, 0.f) : v0, relu ? fmaxf(v1, 0.f) : v1);
+      }
+    }
+  }
+}
+
 // grad of the pre-activation: g_pre = g_post * (pre > 0) (relu) or g_post
 __global__ void k_relu_bwd(const float* gpost, const float* pre, float* gpre, long long n, int relu) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -353,6 +462,23 @@ int launch_conv(const void* x, const void* W, const float* b, float* y, void* ya
 }
 
 template <int CI, int CO>
+int launch_conv_mma(const void* x, const void* W, const float* b, float* y, void* yact, const int n[3], int relu,
+                    cudaStream_t st) {
+  const size_t sm = MmaSmem<CI, CO>::bytes;
+  auto kern = k_conv3_mma<CI, CO>;
+  static bool opted = false;
+  if (!opted) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    opted = true;
+  }
+  // 16-byte rows of the staged arrays: 16-byte aligned activations and weights
+  if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(W)) & 15) return SDNS_EINVAL;
+  const int nblk = (n[0] / BR) * (n[1] / BR) * (n[2] / BR);
+  kern<<<nblk, 256, sm, st>>>((const bf16*)x, (const bf16*)W, b, y, (bf16*)yact, n[0], n[1], n[2], relu);
+  return cudaGetLastError() == cudaSuccess ? SDNS_OK : SDNS_ECUDA;
+}
+
+template <int CI, int CO>
 int launch_wgrad(const void* x, const float* g, float* dW, float* db, const int n[3], cudaStream_t st) {
   const size_t sm = (size_t)(HB * HB * HB * CI + BP * CO) * sizeof(float);
   auto kern = k_conv3_wgrad<CI, CO>;
@@ -437,9 +563,9 @@ int sdns_conv3d_fwd(const void* x, const void* W, const float* b, float* y, void
                     int32_t co, int32_t relu, void* stream) {
   if (!x || !W || !y || !n || !grid_ok(n)) return SDNS_EINVAL;
   cudaStream_t st = (cudaStream_t)stream;
-  if (ci == 16 && co == 32) return launch_conv<bf16, 16, 32, 0>(x, W, b, y, yact, n, relu, st);
-  if (ci == 32 && co == 32) return launch_conv<bf16, 32, 32, 0>(x, W, b, y, yact, n, relu, st);
-  if (ci == 32 && co == 8) return launch_conv<bf16, 32, 8, 0>(x, W, b, y, yact, n, relu, st);
+  if (ci == 16 && co == 32) return launch_conv_mma<16, 32>(x, W, b, y, yact, n, relu, st);
+  if (ci == 32 && co == 32) return launch_conv_mma<32, 32>(x, W, b, y, yact, n, relu, st);
+  if (ci == 32 && co == 8) return launch_conv_mma<32, 8>(x, W, b, y, yact, n, relu, st);
   return SDNS_EINVAL;
 }
 

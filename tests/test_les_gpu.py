@@ -128,15 +128,21 @@ def test_network_gradient_against_oracle(built_lib):
     _ok(built_lib.sdns_mse_grad(_p(y), CPAD_OUT, NOUT, _p(_t(tgt)), P, _p(grad), _p(loss), _stream()))
     net.backward(xd, grad)
     torch.cuda.synchronize()
-    # oracle: same bf16-rounded weights and activations
+    # oracle backpropagation with the same BF16 weights and the same BF16 activations the GPU
+    # forward produced (a different FP32 summation order may round an activation to the
+    # neighbouring BF16 value; the forward itself is checked in test_conv_forward_backward)
     w = net.wb.float().cpu().numpy()
     Ws, bs = [], []
     for li, (ci, co, _) in enumerate(LAYERS):
         Ws.append(w[net.offs[2 * li]:net.offs[2 * li + 1]].reshape(27, co, ci))
         bs.append(net.w.cpu().numpy()[net.offs[2 * li + 1]:net.offs[2 * li + 2]])
     a0 = x.reshape(n + (16,)).astype(np.float64)
-    pre1 = les_ref.conv3d(a0, Ws[0], bs[0]); a1 = _bf16_exact(np.maximum(pre1, 0)).astype(np.float64)
-    pre2 = les_ref.conv3d(a1, Ws[1], bs[1]); a2 = _bf16_exact(np.maximum(pre2, 0)).astype(np.float64)
+    pre1 = net.pre[0].cpu().numpy().reshape(n + (32,)).astype(np.float64)
+    a1 = net.act[0].float().cpu().numpy().reshape(n + (32,)).astype(np.float64)
+    pre2 = net.pre[1].cpu().numpy().reshape(n + (32,)).astype(np.float64)
+    a2 = net.act[1].float().cpu().numpy().reshape(n + (32,)).astype(np.float64)
+    assert np.max(np.abs(pre1 - les_ref.conv3d(a0, Ws[0], bs[0]))) < 2e-5 * np.max(np.abs(pre1))
+    assert np.max(np.abs(pre2 - les_ref.conv3d(a1, Ws[1], bs[1]))) < 2e-5 * np.max(np.abs(pre2))
     pre3 = les_ref.conv3d(a2, Ws[2], bs[2])
     d = np.zeros_like(pre3)
     d[..., :NOUT] = pre3[..., :NOUT] - tgt.reshape(n + (NOUT,))
