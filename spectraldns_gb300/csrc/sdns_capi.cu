@@ -804,7 +804,7 @@ int sdns_create(const sdns_config* cfg, sdns_ctx** out) {
   // twiddle tables: per axis, pass tables [r][k] of W_{Ns R}^{r k} (forward)
   {
     long long tot = 0;
-    for (int i = 0; i < 3; ++i) { c->twoff[i] = tot; tot += tw_len(cfg->n[i]); }
+    for (int i = 0; i < 3; ++i) { c->twoff[i] = tot; tot += tw_total(cfg->n[i]); }
     std::vector<double> h(2 * tot);
     for (int i = 0; i < 3; ++i) {
       const int n = cfg->n[i];
@@ -822,6 +822,11 @@ int sdns_create(const sdns_config* cfg, sdns_ctx** out) {
           }
         off += m;
         ns *= r;
+      }
+      for (int q = 0; q < n; ++q) {  // full table W_n^q
+        const double ang = -2.0 * M_PI * (double)q / (double)n;
+        h[2 * (off + q)] = cos(ang);
+        h[2 * (off + q) + 1] = sin(ang);
       }
     }
     if ((e = dalloc(c, &c->tw, tot * cb))) return bail(e);

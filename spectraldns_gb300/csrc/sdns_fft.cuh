@@ -94,11 +94,38 @@ template <int S, typename C> __device__ __forceinline__ void dft16(C* v) {
   for (int i = 0; i < 16; ++i) v[i] = t[i];
 }
 
+// cos(pi k/16) for k = 0..8; sin(pi k/16) = cos(pi (8-k)/16)
+__host__ __device__ constexpr double c16(int k) {
+  return k == 0 ? 1.0 : k == 1 ? 0.98078528040323044913 : k == 2 ? SDNS_C8 : k == 3 ? 0.83146961230254523708
+       : k == 4 ? SDNS_R2 : k == 5 ? 0.55557023301960222474 : k == 6 ? SDNS_S8 : k == 7 ? 0.19509032201612826785
+       : 0.0;
+}
+__host__ __device__ constexpr double cos16(int k) { return k <= 8 ? c16(k) : -c16(16 - k); }  // k = 0..15
+
+// 32-point DFT in registers: radix 2 over two 16-point DFTs (even / odd inputs),
+// X[k] = E[k] + W32^k O[k], X[k+16] = E[k] - W32^k O[k]; natural order out.
+template <int S, typename C> __device__ __forceinline__ void dft32(C* v) {
+  C e[16], o[16];
+#pragma unroll
+  for (int m = 0; m < 16; ++m) { e[m] = v[2 * m]; o[m] = v[2 * m + 1]; }
+  dft16<S>(e);
+  dft16<S>(o);
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    C t = o[k];
+    if (k == 8) t = mul_si<S>(t);
+    else if (k != 0) t = mulc<S>(t, cos16(k), k < 8 ? c16(8 - k) : c16(k - 8));
+    v[k] = cadd(e[k], t);
+    v[k + 16] = csub(e[k], t);
+  }
+}
+
 template <int R, int S, typename C> __device__ __forceinline__ void dftR(C* v) {
   if constexpr (R == 2) dft2<S>(v[0], v[1]);
   else if constexpr (R == 4) dft4<S>(v[0], v[1], v[2], v[3]);
   else if constexpr (R == 8) dft8<S>(v);
-  else dft16<S>(v);
+  else if constexpr (R == 16) dft16<S>(v);
+  else dft32<S>(v);
 }
 
 // padded shared-memory index of line position p (breaks stride-16 bank conflicts)
@@ -113,6 +140,10 @@ __host__ __device__ inline int tw_len(int n) {
   while (ns < n) { int r = (n / ns) >= 16 ? 16 : n / ns; len += r * ns; ns *= r; }
   return len;
 }
+
+// Each axis's table ends with the full table W_n^m, m = 0..n-1 (forward), which
+// the two-pass radix-32 transforms index directly.
+__host__ __device__ inline int tw_total(int n) { return tw_len(n) + n; }
 
 // One Stockham pass of radix R on a line held in `buf` (padded positions).
 template <int R, int E, int S, typename C>
@@ -407,6 +438,73 @@ __device__ __forceinline__ void first16_buf(C* buf, int g) {
     for (int r = 0; r < R; ++r) b[r] = v[q * R + r];
   }
   __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// Two-pass transforms of N = 512 (32 x 16) and N = 1024 (32 x 32) lines with
+// E = 32 values per lane (G = N/32 lanes per line): a radix-32 first pass and
+// a radix-N/32 last pass.  One shared-memory round trip fewer than 16,16,2 /
+// 16,16,4, so fewer shared-memory instructions and a shorter dependency chain.
+// The last pass reads its twiddles W_N^{r k} from the full table `twf`
+// (FP32: the powers of k from log2(R) loads; FP64: one load each).
+// ---------------------------------------------------------------------------
+template <int N, int S, bool PR, typename C>
+__device__ __forceinline__ void first32_buf(C* buf, int g) {
+  constexpr int NR = N / 32;  // 16 or 32: a multiple of 16
+  static_assert(NR % 16 == 0, "radix-32 first pass for N = 512, 1024");
+  C v[32];
+  const C* b = buf + padp(g);
+#pragma unroll
+  for (int r = 0; r < 32; ++r) v[r] = (PR && r >= 12 && r <= 19) ? mk<C>(0, 0) : b[r * pstride<NR>()];
+  __syncwarp();
+  dft32<S>(v);
+  C* o = buf + 34 * g;  // padp(32 g + r) = 34 g + r + r/16
+#pragma unroll
+  for (int r = 0; r < 32; ++r) o[r + (r >> 4)] = v[r];
+  __syncwarp();
+}
+
+template <int N, int S, typename C>
+__device__ __forceinline__ void last32_buf(C* buf, int g, const C* __restrict__ twf) {
+  constexpr int R = N / 32, E = 32, NB = E / R, NR = N / R, G = N / 32, Ns = 32;
+  C v[E];
+#pragma unroll
+  for (int q = 0; q < NB; ++q) load_r<R, NR>(buf, g + G * q, padq<G>(g, q), &v[q * R]);
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const int k = (g + G * q) & (Ns - 1);
+    C w[R];
+    if constexpr (sizeof(C) == 8) {
+#pragma unroll
+      for (int b = 1; b < R; b <<= 1) w[b] = twf[k * b];
+#pragma unroll
+      for (int r = 3; r < R; ++r) {
+        if ((r & (r - 1)) == 0) continue;
+        int hb = 1;
+        while (hb * 2 <= r) hb *= 2;
+        w[r] = cmul(w[r - hb], w[hb]);
+      }
+    } else {
+#pragma unroll
+      for (int r = 1; r < R; ++r) w[r] = twf[k * r];
+    }
+#pragma unroll
+    for (int r = 1; r < R; ++r) v[q * R + r] = cmul(v[q * R + r], S > 0 ? cconj(w[r]) : w[r]);
+    dftR<R, S>(&v[q * R]);
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const int j = g + G * q;  // j < Ns: the output block starts at j
+    store_r<R, Ns>(buf, j, &v[q * R]);
+  }
+  __syncwarp();
+}
+
+template <int N, int S, bool PR, typename C>
+__device__ __forceinline__ void line_fft_r32(C* buf, int g, const C* __restrict__ tw) {
+  first32_buf<N, S, PR>(buf, g);
+  last32_buf<N, S>(buf, g, tw + tw_len(N));
 }
 
 // Same transform with the line length N fixed at compile time: the pass

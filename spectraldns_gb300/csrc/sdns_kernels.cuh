@@ -57,11 +57,17 @@ __host__ __device__ inline int tile_pitch(int minlen, int W, int csz) {
 }
 __host__ __device__ inline int axis_ld(int n, int W, int csz) { return tile_pitch(n + ((n - 1) >> 4), W, csz); }
 
+// FP32 lines of 512 and 1024 points use the two-pass radix-32 transforms
+template <typename Real, int N> struct axis_r32 {
+  static constexpr bool value = sizeof(Real) == 4 && (N == 512 || N == 1024);
+};
+
 template <typename Real, int N, int S>
-__global__ void __launch_bounds__(256, 3) k_axis_p(AxisArgs a) {
+__global__ void __launch_bounds__(256, axis_r32<Real, N>::value ? 2 : 3) k_axis_p(AxisArgs a) {
   using C = typename cplx_of<Real>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
-  constexpr int E = axis_e<N>::value, G = N / E;
+  constexpr bool R32 = axis_r32<Real, N>::value;
+  constexpr int E = R32 ? 32 : axis_e<N>::value, G = N / E;
   const int W = blockDim.x / G, LD = axis_ld(N, W, (int)sizeof(C));
   const int wsh = __ffs(W) - 1;
   C* const bufs = reinterpret_cast<C*>(smraw);
@@ -118,8 +124,13 @@ __global__ void __launch_bounds__(256, 3) k_axis_p(AxisArgs a) {
       cp_wait_all();
     }
     __syncthreads();
-    if (prune) line_fft_t<N, E, S, true>(cur + wl * LD, g, tw);
-    else line_fft_t<N, E, S, false>(cur + wl * LD, g, tw);
+    if constexpr (R32) {
+      if (prune) line_fft_r32<N, S, true>(cur + wl * LD, g, tw);
+      else line_fft_r32<N, S, false>(cur + wl * LD, g, tw);
+    } else {
+      if (prune) line_fft_t<N, E, S, true>(cur + wl * LD, g, tw);
+      else line_fft_t<N, E, S, false>(cur + wl * LD, g, tw);
+    }
     __syncthreads();
     {
       C* out = reinterpret_cast<C*>(a.out) + (long long)f * a.out_fs;
@@ -995,9 +1006,11 @@ inline size_t smem_limit() {
 template <typename Real, int N, int S>
 static int launch_axis_p(const AxisArgs& a, cudaStream_t s) {
   using C = typename cplx_of<Real>::type;
-  constexpr int G = N / axis_e<N>::value;
+  constexpr bool R32 = axis_r32<Real, N>::value;
+  constexpr int G = N / (R32 ? 32 : axis_e<N>::value);
   const size_t lim = smem_limit();
-  int W = 256 / G;
+  // 8-line tiles (64-byte rows at FP32): 128 threads with 16 lanes per line at N = 512
+  int W = (R32 && N == 512 ? 128 : 256) / G;
   while (W > 2 && (size_t)2 * W * axis_ld(N, W, (int)sizeof(C)) * sizeof(C) > lim) W >>= 1;
   const size_t sm = (size_t)2 * W * axis_ld(N, W, (int)sizeof(C)) * sizeof(C);
   auto kern = k_axis_p<Real, N, S>;

@@ -68,7 +68,16 @@ struct NaGeo {
 template <typename C>
 __global__ void k_na_twiddles(C* tw, int n) {
   const int len = tw_len(n);
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < len; e += gridDim.x * blockDim.x) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < tw_total(n); e += gridDim.x * blockDim.x) {
+    if (e >= len) {  // full table W_n^q
+      double sn, cs;
+      sincospi(-2.0 * (double)(e - len) / (double)n, &sn, &cs);
+      C w;
+      w.x = (decltype(w.x))cs;
+      w.y = (decltype(w.x))sn;
+      tw[e] = w;
+      continue;
+    }
     int ns = 1, off = 0;
     while (true) {
       const int r = (n / ns) >= 16 ? 16 : n / ns;
@@ -149,7 +158,7 @@ NaLayout na_layout(const int n[3], long long K0, long long K1, long long Kzp, si
   size_t off = 0;
   for (int i = 0; i < 3; ++i) {
     L.tw[i] = off;
-    off = (size_t)rup((long long)(off + (size_t)tw_len(n[i]) * csz), 256);
+    off = (size_t)rup((long long)(off + (size_t)tw_total(n[i]) * csz), 256);
   }
   L.dt = off;
   off += 256;
