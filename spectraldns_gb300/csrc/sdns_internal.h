@@ -64,6 +64,7 @@ struct AxisArgs {
   double kscale[3];
   RowMap m1;                 // rows of axis 1 (for k1 of the batch index)
   int Kzp;
+  int nbuf;                  // tile buffers of the persistent sweep (set by its launcher: 1 or 2)
 };
 
 // Fused z-line sweep: C2R of 6 spectral fields, u x w, R2C of 3 fields.

@@ -109,15 +109,19 @@ __global__ void __launch_bounds__(256, axis_r32<Real, N>::value ? 2 : 3) k_axis_
     cp_commit();
   };
   const unsigned gstep = gridDim.x;
+  const bool dbuf = a.nbuf == 2;  // double buffering: the next tile is in flight during this one
   unsigned task = blockIdx.x;
   unsigned f = task / ntile, tile = task - f * ntile;
   int b = 0;
-  if (task < ntask) issue(f, tile, bufs);
-  for (; task < ntask; task += gstep, b ^= 1) {
+  if (task < ntask && dbuf) issue(f, tile, bufs);
+  for (; task < ntask; task += gstep, b ^= (dbuf ? 1 : 0)) {
     C* const cur = bufs + (size_t)b * W * LD;
     unsigned nf = f, ntl = tile + gstep;
     while (ntl >= ntile) { ntl -= ntile; ++nf; }
-    if (task + gstep < ntask) {
+    if (!dbuf) {
+      issue(f, tile, cur);
+      cp_wait_all();
+    } else if (task + gstep < ntask) {
       issue(nf, ntl, bufs + (size_t)(b ^ 1) * W * LD);
       asm volatile("cp.async.wait_group 1;\n" ::: "memory");
     } else {
@@ -174,7 +178,7 @@ __global__ void __launch_bounds__(256, axis_r32<Real, N>::value ? 2 : 3) k_axis_
         }
       }
     }
-    __syncthreads();  // cur is refilled two tasks ahead
+    __syncthreads();  // cur is refilled (double buffering: two tasks ahead)
     f = nf;
     tile = ntl;
   }
@@ -188,7 +192,7 @@ __host__ __device__ inline int staged_rows(int rin, int W, int csz) {
 }
 
 template <typename Real, int N>
-__global__ void __launch_bounds__(256, 2) k_axis_curl6(AxisArgs a) {
+__global__ void __launch_bounds__(512, 1) k_axis_curl6(AxisArgs a) {
   using C = typename cplx_of<Real>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   constexpr int E = axis_e<N>::value, G = N / E;
@@ -1009,10 +1013,15 @@ static int launch_axis_p(const AxisArgs& a, cudaStream_t s) {
   constexpr bool R32 = axis_r32<Real, N>::value;
   constexpr int G = N / (R32 ? 32 : axis_e<N>::value);
   const size_t lim = smem_limit();
-  // 8-line tiles (64-byte rows at FP32): 128 threads with 16 lanes per line at N = 512
-  int W = (R32 && N == 512 ? 128 : 256) / G;
-  while (W > 2 && (size_t)2 * W * axis_ld(N, W, (int)sizeof(C)) * sizeof(C) > lim) W >>= 1;
-  const size_t sm = (size_t)2 * W * axis_ld(N, W, (int)sizeof(C)) * sizeof(C);
+  // 256 threads.  Radix-32 sweeps: 16-line tiles (128-byte rows at FP32 N = 512), one tile
+  // buffer, two blocks per SM (measured faster than 8-line tiles double buffered, and than
+  // 16-line tiles double buffered at one block per SM).  Others: double buffered.
+  int W = 256 / G;
+  const int nbuf = R32 ? 1 : 2;
+  while (W > 2 && (size_t)nbuf * W * axis_ld(N, W, (int)sizeof(C)) * sizeof(C) > lim) W >>= 1;
+  const size_t sm = (size_t)nbuf * W * axis_ld(N, W, (int)sizeof(C)) * sizeof(C);
+  AxisArgs args = a;
+  args.nbuf = nbuf;
   auto kern = k_axis_p<Real, N, S>;
   int dev = 0, nsm = 148, occ = 1;
   cudaGetDevice(&dev);
@@ -1024,7 +1033,7 @@ static int launch_axis_p(const AxisArgs& a, cudaStream_t s) {
   long long nb = (long long)occ * nsm;
   if (nb > ntask) nb = ntask;
   if (nb < 1) return 0;
-  kern<<<(unsigned)nb, W * G, sm, s>>>(a);
+  kern<<<(unsigned)nb, W * G, sm, s>>>(args);
   return (int)cudaGetLastError();
 }
 
@@ -1058,7 +1067,7 @@ static int launch_curl6(const AxisArgs& a, cudaStream_t s) {
     return (size_t)w * ((size_t)3 * staged_rows(rin, w, cs) + axis_ld(N, w, cs)) * sizeof(C);
   };
   const size_t lim = smem_limit();
-  int W = 256 / G;
+  int W = 512 / G;  // 16-line tiles at N = 512 (128-byte rows), halved while they do not fit
   while (W > 2 && bytes(W) > lim) W >>= 1;
   const size_t sm = bytes(W);
   k_axis_curl6<Real, N><<<(unsigned)((a.nlines + W - 1) / W), W * G, sm, s>>>(a);
