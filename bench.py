@@ -225,6 +225,14 @@ def run_ours(args):
                 "step_alg_bytes": step_bytes,
                 "step_achieved_gbs": step_bytes / (ms / args.steps * 1e-3) / 1e9}
     roofline["step_frac"] = roofline["step_achieved_gbs"] / peak
+    # the same step against the full-spectral-array byte model 4 (27 + 9a) F per step,
+    # F = 8 N0 N1 (N2/2+1): a = 2 for 16-byte accumulators (this build's compensated FP32 S, A),
+    # a = 1 for 8-byte ones; this build stores only the kept modes and moves fewer bytes
+    F = 8.0 * N[0] * N[1] * (N[2] // 2 + 1)
+    t_step = ms / args.steps * 1e-3
+    roofline["full_array_model"] = {
+        "bytes_per_step_a2": 4 * (27 + 18) * F, "frac_a2": 4 * (27 + 18) * F / t_step / 1e9 / peak,
+        "bytes_per_step_a1": 4 * (27 + 9) * F, "frac_a1": 4 * (27 + 9) * F / t_step / 1e9 / peak}
     launches = sum(klaunch) + args.steps * 3  # + step-begin, CFL dt and step-end kernels
 
     out = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
