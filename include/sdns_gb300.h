@@ -126,6 +126,25 @@ int sdns_divergence(sdns_ctx* ctx, const void* u_hat, void* div, int where);
 int sdns_diagnostics(sdns_ctx* ctx, double* out /* SDNS_DIAG_COUNT */);
 int sdns_spectrum(sdns_ctx* ctx, double* Ek, int32_t nbins);
 
+/* ---- integrator building blocks (spectralDNS/maths/integrators.py:15-147
+ * adaptiveRK, :161-165 ForwardEuler, :167-175 AB2, driven from the host as
+ * getintegrator :177-239 does).  The stage arrays of these
+ * integrators stay on the GPU: every pointer is device memory of the context's
+ * GPU holding a spectral vector (3, N0, N1, N2/2+1) of the context precision;
+ * both run on the context stream. ---- */
+#define SDNS_LINCOMB_MAX 8
+/* out = base + sum_k coef[k] * terms[k] (k < nterms <= SDNS_LINCOMB_MAX;
+ * base NULL: 0), summed term by term in the working precision as the
+ * reference's `u0_new += dt*b[j]*fY_hat[j]` updates (integrators.py:66-68,
+ * 78-84, 164, 171-174).  out may alias base or a term. */
+int sdns_lincomb(sdns_ctx* ctx, void* out, const void* base, int32_t nterms, const double* coef,
+                 const void* const* terms);
+/* float64 sums[k] = sum over component k of |err/sc|^2 with
+ * sc = atol + max(|u0|, |u1|) * rtol (integrators.py:87-92, errnorm "2");
+ * synchronous (the adaptive step needs the estimate on the host). */
+int sdns_error_norm(sdns_ctx* ctx, const void* err, const void* u0, const void* u1, double atol, double rtol,
+                    double* sums /* 3 */);
+
 /* device time (ms) of the kernels of the last sdns_rk4 call, per kernel
  * class, measured with CUDA events on the context stream when timing is on */
 int sdns_set_timing(sdns_ctx* ctx, int32_t on);

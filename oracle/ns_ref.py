@@ -18,6 +18,9 @@ What it restates (paths relative to the spectralDNS source tree):
 * ``spectralDNS/solvers/NS.py:219-261``  ComputeRHS (``rhs += Source``, :259).
 * ``spectralDNS/maths/integrators.py:149-159, 185-186``  classic RK4 with
   ``a=[1/6,1/3,1/3,1/6]``, ``b=[1/2,1/2,1]``.
+* ``spectralDNS/maths/integrators.py:15-147, 161-175, 193-233`` ForwardEuler,
+  AB2 and the embedded Runge-Kutta step (FSAL, error norm "2", step-size
+  controller) with the Bogacki-Shampine 5(4) tableau (``Integrator``).
 * ``spectralDNS3D_short.py:36-46, 76-86`` and ``cpp/spectralDNS.cpp:122-129,
   217-236``  the explicit 2/3 rule: keep modes with ``|k_i| < (2/3)(N_i/2+1)``
   on every axis (integer wave index), applied to the nonlinear term on
@@ -261,6 +264,116 @@ class Grid:
         if Ef > 0:
             src[:] = (eps / (2.0 * Ef)) * uh * shell
         return src
+
+
+# Bogacki-Shampine 5(4) pair (P. Bogacki, L. F. Shampine, Comput. Math. Appl.
+# 32 (1996) 15-28), as tabulated at spectralDNS/maths/integrators.py:197-209:
+# 8 stages, first-same-as-last, embedded order 4.
+_BS5_ROWS = (
+    (),
+    ("1/6",),
+    ("2/27", "4/27"),
+    ("183/1372", "-162/343", "1053/1372"),
+    ("68/297", "-4/11", "42/143", "1960/3861"),
+    ("597/22528", "81/352", "63099/585728", "58653/366080", "4617/20480"),
+    ("174197/959244", "-30942/79937", "8152137/19744439", "666106/1039181", "-29421/29068", "482048/414219"),
+    ("587/8064", "0", "4440339/15491840", "24353/124800", "387/44800", "2152/5985", "7267/94080"),
+)
+_BS5_BHAT = ("2479/34992", "0", "123/416", "612941/3411720", "43/1440", "2272/6561", "79937/1113912", "3293/556956")
+
+
+def bs5_tableau(dtype=np.float64):
+    """(A, b, bhat) of the BS5 pair in ``dtype`` (integrators.py:197-211)."""
+    from fractions import Fraction
+    A = np.zeros((8, 8))
+    for i, row in enumerate(_BS5_ROWS):
+        for j, q in enumerate(row):
+            A[i, j] = float(Fraction(q))
+    b = A[7].copy()  # the last stage is the solution (FSAL)
+    bhat = np.array([float(Fraction(q)) for q in _BS5_BHAT])
+    return A.astype(dtype), b.astype(dtype), bhat.astype(dtype)
+
+
+class Integrator:
+    """The non-RK4 integrators of spectralDNS/maths/integrators.py on the oracle grid.
+
+    ``step(uh, dt, tstep)`` returns ``(uh_new, dt_next, dt_taken)`` like the
+    reference's integrator closures (getintegrator :177-239):
+
+    * ``ForwardEuler`` (:161-165): ``u += dt F(u)``.
+    * ``AB2`` (:167-175): ``u += dt F(u)`` on the first step, then
+      ``u += 1.5 dt F(u) - 0.5 (dt F)_previous``.
+    * ``BS5_fixed`` / ``BS5_adaptive`` (:15-147 with aTOL = rTOL = TOL):
+      FSAL stage reuse through the rotating ``offset``, error norm "2"
+      ``max_k sqrt(sum |err_k/sc_k|^2) / sqrt(prod(spectral shape))`` and, when
+      adaptive, the step-size controller ``fac=0.8, facmin=0.01, facmax=2``
+      (1 after a rejection) with exponent 1/(err_order+1).
+    """
+
+    def __init__(self, grid: Grid, name: str, tol: float = 1e-6, source=None):
+        self.g = grid
+        self.name = name
+        self.tol = tol
+        self.source = source
+        self.prev = None  # AB2: dt F of the previous step
+        if name.startswith("BS5"):
+            self.A, self.b, self.bhat = bs5_tableau(grid.dtype)
+            self.fY = np.zeros((8, 3) + grid.spec_shape, dtype=grid.cdtype)
+            self.offset = 0
+        elif name not in ("ForwardEuler", "AB2"):
+            raise ValueError(name)
+        self.rejected = 0
+
+    def F(self, u):
+        return self.g.compute_rhs(u, self.source)
+
+    def step(self, uh, dt, tstep):
+        dtype = self.g.dtype
+        if self.name == "ForwardEuler":
+            return uh + self.F(uh) * dtype.type(dt), dt, dt
+        if self.name == "AB2":
+            rhs = self.F(uh)
+            if tstep == 0:
+                new = uh + rhs * dtype.type(dt)
+            else:
+                new = uh + (dtype.type(1.5) * rhs * dtype.type(dt) - dtype.type(0.5) * self.prev)
+            self.prev = rhs * dtype.type(dt)
+            return new, dt, dt
+        return self._adaptive(uh, dt, tstep, adaptive=self.name == "BS5_adaptive")
+
+    def _adaptive(self, u0, dt, tstep, adaptive):
+        A, b, bhat, fY = self.A, self.b, self.bhat, self.fY
+        s = 8
+        facmax, fac, facmin = 2.0, 0.8, 0.01
+        exponent = 1.0 / (4 + 1)
+        while True:
+            dt_prev = dt
+            self.offset = (self.offset - 1) % s
+            o = self.offset
+            for i in range(s):
+                if tstep == 0 or i != 0:
+                    y = u0.copy()
+                    for j in range(i):
+                        y += dt * A[i, j] * fY[(j + o) % s]
+                    fY[(i + o) % s] = self.F(y)
+            u_new = u0.copy()
+            err = np.zeros_like(u0)
+            for j in range(s):
+                u_new += dt * b[j] * fY[(j + o) % s]
+                err += dt * (b[j] - bhat[j]) * fY[(j + o) % s]
+            sc = self.tol + np.maximum(np.abs(u0), np.abs(u_new)) * self.tol
+            nsq = [np.sum(np.abs(err[k].astype(np.complex128) / sc[k]) ** 2) for k in range(3)]
+            est = float(np.max(np.sqrt(nsq))) / math.sqrt(float(np.prod(self.g.spec_shape)))
+            factor = min(facmax, max(facmin, fac * (1.0 / est) ** exponent))
+            if adaptive:
+                dt = dt * factor
+                if est > 1.0:
+                    facmax = 1.0
+                    self.rejected += 1
+                    self.offset += 1
+                    continue
+            self.last_est = est
+            return u_new, dt, dt_prev
 
 
 def taylor_green(grid: Grid):

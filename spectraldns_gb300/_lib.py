@@ -16,6 +16,7 @@ SDNS_DEALIAS_23, SDNS_DEALIAS_NONE = 0, 1
 SDNS_HOST, SDNS_DEVICE = 0, 1
 DIAG_NAMES = ("energy", "enstrophy", "dissipation", "divergence", "cfl_rate", "time", "last_dt")
 SDNS_DIAG_COUNT = 8
+SDNS_LINCOMB_MAX = 8
 
 
 class sdns_config(C.Structure):
@@ -66,6 +67,8 @@ SIGNATURES = {
     "sdns_spectrum": (C.c_int, [_CTX, C.POINTER(C.c_double), C.c_int32]),
     "sdns_set_timing": (C.c_int, [_CTX, C.c_int32]),
     "sdns_get_timing": (C.c_int, [_CTX, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
+    "sdns_lincomb": (C.c_int, [_CTX, _P, _P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_void_p)]),
+    "sdns_error_norm": (C.c_int, [_CTX, _P, _P, _P, C.c_double, C.c_double, C.POINTER(C.c_double)]),
     "sdns_compute_rhs_noalloc": (C.c_int, [C.POINTER(sdns_config), _P, _P, _P]),
     # learned-closure LES
     "sdns_les_box_filter": (C.c_int, [_P, C.c_int32, _P, C.c_int32, _P, _P, _P]),

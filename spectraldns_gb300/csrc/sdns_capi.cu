@@ -103,6 +103,7 @@ struct sdns_ctx {
   double* partials = nullptr;
   long long nblk_rk = 0;
   int* flag = nullptr;
+  double* red = nullptr;     // per-block partial sums of sdns_error_norm
   // host state
   double eps = 0, kf = 0, cfl = 0, last_dt = -1;
   bool has_state = false;
@@ -465,6 +466,70 @@ __global__ void k_spectrum(const void* Sv, const C* H, Geo g, long long ncomp1, 
                                  (double)c.x * c.x + (double)c.y * c.y));
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// integrator kernels: the linear combinations and the error estimate of the
+// ForwardEuler, AB2 and embedded Runge-Kutta (BS5) steps of
+// spectralDNS/maths/integrators.py:15-147, 161-175 on caller-layout vectors
+// ---------------------------------------------------------------------------
+struct LinTerms {
+  const void* t[SDNS_LINCOMB_MAX];
+  double c[SDNS_LINCOMB_MAX];
+  int n;
+};
+
+// out = base + sum_k c_k t_k, accumulated term by term in the working
+// precision (the order of the reference's `u += c*t` updates)
+template <typename C>
+__global__ void k_lincomb(C* out, const C* base, LinTerms lt, long long count) {
+  using Real = decltype(C::x);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+    Real x = 0, y = 0;
+    if (base) {
+      const C b = base[i];
+      x = b.x;
+      y = b.y;
+    }
+#pragma unroll
+    for (int k = 0; k < SDNS_LINCOMB_MAX; ++k) {
+      if (k < lt.n) {
+        const C v = reinterpret_cast<const C*>(lt.t[k])[i];
+        const Real ck = (Real)lt.c[k];
+        x += ck * v.x;
+        y += ck * v.y;
+      }
+    }
+    out[i] = mk<C>(x, y);
+  }
+}
+
+// per-block float64 sums over each of the 3 components of |err / sc|^2 with
+// sc = atol + max(|u0|, |u1|) rtol (integrators.py:87-92)
+template <typename C>
+__global__ void __launch_bounds__(256) k_err_norm(const C* err, const C* u0, const C* u1, double atol, double rtol,
+                                                  long long n1, double* part) {
+  __shared__ double red[3][256];
+  double s[3] = {0, 0, 0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < 3 * n1; i += (long long)gridDim.x * blockDim.x) {
+    const C e = err[i], a = u0[i], b = u1[i];
+    const double ma = hypot((double)a.x, (double)a.y), mb = hypot((double)b.x, (double)b.y);
+    const double sc = atol + fmax(ma, mb) * rtol;
+    const double v = ((double)e.x * e.x + (double)e.y * e.y) / (sc * sc);
+    const int q = (int)(i / n1);
+    s[0] += q == 0 ? v : 0.0;
+    s[1] += q == 1 ? v : 0.0;
+    s[2] += q == 2 ? v : 0.0;
+  }
+  for (int q = 0; q < 3; ++q) red[q][threadIdx.x] = s[q];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 3; ++q) part[3 * blockIdx.x + q] = red[q][0];
 }
 
 // ---------------------------------------------------------------------------
@@ -853,7 +918,7 @@ int sdns_destroy(sdns_ctx* c) {
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   void* bufs[] = {c->Y, c->S, c->A, c->T1, c->T2, c->Pc, c->Yx, c->src, c->src_full, c->H,
-                  c->F1, c->F2, c->PH, c->stage, c->tw, c->sc, c->partials, c->flag};
+                  c->F1, c->F2, c->PH, c->stage, c->tw, c->sc, c->partials, c->flag, c->red};
   for (void* p : bufs)
     if (p) cudaFree(p);
   for (auto& e : c->evpool)
@@ -1205,6 +1270,51 @@ int sdns_spectrum(sdns_ctx* c, double* Ek, int32_t nbins) {
     const double k0 = i + 0.5, k = i + 1.5;
     Ek[i] = (h[nbins + i] > 0 && i < nbins - 1) ? (4.0 / 3.0 * M_PI) * (k * k * k - k0 * k0 * k0) * h[i] / h[nbins + i] : 0.0;
   }
+  return SDNS_OK;
+}
+
+int sdns_lincomb(sdns_ctx* c, void* out, const void* base, int32_t nterms, const double* coef,
+                 const void* const* terms) {
+  int e = check_ctx(c);
+  if (e) return e;
+  if (!out || nterms < 0 || nterms > SDNS_LINCOMB_MAX || (nterms > 0 && (!coef || !terms)))
+    return fail(SDNS_EINVAL, "sdns_lincomb: bad arguments (0 <= nterms <= %d)", SDNS_LINCOMB_MAX);
+  LinTerms lt = {};
+  lt.n = nterms;
+  for (int k = 0; k < nterms; ++k) {
+    if (!terms[k]) return fail(SDNS_EINVAL, "sdns_lincomb: null term %d", k);
+    lt.t[k] = terms[k];
+    lt.c[k] = coef[k];
+  }
+  const long long n = 3 * c->nfull1;
+  if (c->dbl)
+    k_lincomb<double2><<<nblocks(n), 256, 0, c->st>>>((double2*)out, (const double2*)base, lt, n);
+  else
+    k_lincomb<float2><<<nblocks(n), 256, 0, c->st>>>((float2*)out, (const float2*)base, lt, n);
+  CK(cudaGetLastError());
+  return SDNS_OK;
+}
+
+int sdns_error_norm(sdns_ctx* c, const void* err, const void* u0, const void* u1, double atol, double rtol,
+                    double* sums) {
+  int e = check_ctx(c);
+  if (e) return e;
+  if (!err || !u0 || !u1 || !sums) return fail(SDNS_EINVAL, "sdns_error_norm: null argument");
+  const unsigned nb = 152 * 2;
+  if (!c->red && (e = dalloc(c, &c->red, 3LL * nb * 8))) return e;
+  if (c->dbl)
+    k_err_norm<double2><<<nb, 256, 0, c->st>>>((const double2*)err, (const double2*)u0, (const double2*)u1, atol, rtol,
+                                               c->nfull1, c->red);
+  else
+    k_err_norm<float2><<<nb, 256, 0, c->st>>>((const float2*)err, (const float2*)u0, (const float2*)u1, atol, rtol,
+                                              c->nfull1, c->red);
+  CK(cudaGetLastError());
+  std::vector<double> h(3 * nb);
+  CK(cudaMemcpyAsync(h.data(), c->red, 3 * nb * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  for (int q = 0; q < 3; ++q) sums[q] = 0;
+  for (unsigned b = 0; b < nb; ++b)
+    for (int q = 0; q < 3; ++q) sums[q] += h[3 * b + q];
   return SDNS_OK;
 }
 

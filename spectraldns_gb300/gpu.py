@@ -248,6 +248,47 @@ class Context:
         check(self._L.sdns_spectrum(self._h, buf, nbins))
         return np.array(buf[:])
 
+    # -- integrator building blocks (device spectral vectors) ---------------------
+    def _dev_vec(self, t, name):
+        if not (_is_torch(t) and t.is_cuda):
+            raise ValueError("%s must be a CUDA tensor" % name)
+        if t.device.index != self.device or not t.is_contiguous() or t.dtype != _torch_dtype(self.complex) \
+                or tuple(t.shape) != self.spec_shape:
+            raise ValueError("%s must be a contiguous %s tensor of shape %s on cuda:%d"
+                             % (name, np.dtype(self.complex).name, self.spec_shape, self.device))
+        return t.data_ptr()
+
+    def lincomb(self, out, base, coefs, terms):
+        """out = base + sum_k coefs[k] * terms[k] on device spectral vectors (base None: 0).
+
+        Enqueued on the context stream after the work pending on torch's
+        current stream (which may still be writing the operands), like every
+        other call of the context that takes device tensors.
+        """
+        n = len(terms)
+        torch.cuda.current_stream(out.device).synchronize()
+        if n != len(coefs) or n > _lib.SDNS_LINCOMB_MAX:
+            raise ValueError("at most %d terms, one coefficient each" % _lib.SDNS_LINCOMB_MAX)
+        po = self._dev_vec(out, "out")
+        pb = self._dev_vec(base, "base") if base is not None else None
+        ptrs = (C.c_void_p * max(n, 1))(*[self._dev_vec(t, "term") for t in terms])
+        cf = (C.c_double * max(n, 1))(*[float(c) for c in coefs])
+        check(self._L.sdns_lincomb(self._h, C.c_void_p(po), C.c_void_p(pb) if pb else None, n, cf, ptrs))
+        return out
+
+    def error_norm(self, err, u0, u1, atol, rtol):
+        """float64 [sum_k |err/sc|^2 for k = 0, 1, 2], sc = atol + max(|u0|, |u1|) rtol."""
+        sums = (C.c_double * 3)()
+        torch.cuda.current_stream(err.device).synchronize()
+        check(self._L.sdns_error_norm(self._h, C.c_void_p(self._dev_vec(err, "err")),
+                                      C.c_void_p(self._dev_vec(u0, "u0")), C.c_void_p(self._dev_vec(u1, "u1")),
+                                      float(atol), float(rtol), sums))
+        return np.array(sums[:])
+
+    def empty_vec(self):
+        """Uninitialised device spectral vector of the context precision (a torch CUDA tensor)."""
+        return torch.empty(self.spec_shape, dtype=_torch_dtype(self.complex), device="cuda:%d" % self.device)
+
     def memory_bytes(self):
         b = C.c_int64()
         check(self._L.sdns_memory_bytes(self._h, C.byref(b)))

@@ -25,6 +25,7 @@ import numpy as np
 from .. import config
 from ..config import AttributeDict
 from ..gpu import Context
+from ..h5io import HDF5File, init_from_file  # noqa: F401
 from ..utilities import MemoryUsage, Timer, create_profile, reset_profile  # noqa: F401
 
 
@@ -143,42 +144,17 @@ class Space:
         return u_hat
 
 
-class NSFile:
-    """Checkpoint / results writer of the time loop (h5io/HDF5File.py:64-120).
+class NSFile(HDF5File):
+    """Checkpoint / results files of the NS solver (h5io/HDF5File.py; the
+    reference's NS.py:66-70 stores U_hat as the checkpoint and U, P as results).
 
-    h5py is not available, so checkpoints are written as ``<filename>_c.npz``
-    (U_hat, t, tstep) and results as ``<filename>_w.npz``; a file named
-    ``killspectraldns`` in the working directory writes a checkpoint and stops
-    the run (HDF5File.py:107-120).
+    With ``--gpu_sync lazy`` the checkpoint first pulls the state from the GPU.
     """
 
-    def __init__(self, filename, checkpoint=None, results=None):
-        self.filename = filename
-        self.checkpoint = checkpoint or {"data": {}}
-        self.results = results or {"data": {}}
-        self.update_components = lambda **context: None
-
-    def _write_checkpoint(self, params, **context):
-        U_hat = _fresh(context["U_hat"], context.get("gpu"))
-        np.savez(self.filename + "_c.npz", U_hat=np.asarray(U_hat), t=params.t, tstep=params.tstep)
-
-    def update(self, params, **context):
-        if os.path.exists("killspectraldns"):
-            self._write_checkpoint(params, **context)
-            os.remove("killspectraldns")
-            print("killspectraldns found: checkpoint written, stopping")
-            sys.exit(1)
-        if params.tstep % params.checkpoint == 0:
-            self._write_checkpoint(params, **context)
-        if params.tstep % params.write_result == 0:
-            self.update_components(**context)
-            arrays = {}
-            for name, val in self.results["data"].items():
-                arrays[name] = np.asarray(val[0])
-            np.savez(self.filename + "_w_%d.npz" % params.tstep, t=params.t, **arrays)
-
-    def close(self):
-        pass
+    def refresh(self, **context):
+        for fields in self.checkpoint.get("data", {}).values():
+            for val in fields.values():
+                _fresh(val[0], context.get("gpu"))
 
 
 class _Work(dict):
@@ -347,24 +323,55 @@ def ComputeRHS(rhs, u_hat, solver, work=None, Tp=None, VTp=None, P_hat=None, K=N
 
 # ---------------------------------------------------------------- integrator
 def getintegrator(rhs, u0, solver, context):
-    """RK4 on the GPU (maths/integrators.py:149-159, 177-191)."""
-    if params.integrator != "RK4":
-        raise NotImplementedError("the GB300 backend integrates with RK4 only (got %s)" % params.integrator)
+    """The integrator closure of maths/integrators.py:177-239 on the GPU.
+
+    RK4 (:149-159) runs as ``sdns_rk4`` on the library's compact state (one
+    CUDA graph per step).  ForwardEuler, AB2, BS5_fixed and BS5_adaptive run
+    as spectraldns_gb300.integrators.DeviceIntegrator, whose stage vectors
+    stay on the GPU; after every step the library state is set to the new
+    solution, so the getters and diagnostics see it.
+    """
     gpu = context.gpu
     _push_source(gpu, context.get("Source"))
     lazy = params.get("gpu_sync", "step") == "lazy"
     state = {"uploaded": False}
+    if params.integrator == "RK4":
+        def func():
+            if not lazy or not state["uploaded"]:
+                gpu.set_state(u0)
+                state["uploaded"] = True
+            gpu.rk4(float(params.dt), 1)
+            if not lazy:
+                gpu.get_state(out=u0)
+            else:
+                gpu.host_U_hat = u0
+                gpu.host_stale = True
+            return u0, params.dt, params.dt
+        func.__name__ = "RK4"
+        return func
+
+    import torch
+    from ..integrators import DeviceIntegrator
+
+    def callback(fu0):
+        context.fu0 = fu0
+        solver.additional_callback(context)
+
+    integ = DeviceIntegrator(gpu, params.integrator, tol=params.get("TOL", 1e-6), callback=callback)
+    context.integrator = integ
 
     def func():
         if not lazy or not state["uploaded"]:
-            gpu.set_state(u0)
+            integ.u.copy_(torch.from_numpy(np.ascontiguousarray(u0)))
+            torch.cuda.current_stream(integ.u.device).synchronize()
             state["uploaded"] = True
-        gpu.rk4(float(params.dt), 1)
+        dt, dt_took = integ.step(float(params.dt), int(params.tstep))
+        gpu.set_state(integ.u)
         if not lazy:
             gpu.get_state(out=u0)
         else:
             gpu.host_U_hat = u0
             gpu.host_stale = True
-        return u0, params.dt, params.dt
-    func.__name__ = "RK4"
+        return u0, dt, dt_took
+    func.__name__ = params.integrator
     return func

@@ -56,15 +56,36 @@ def test_checkpoint_and_kill_file(tmp_path, monkeypatch):
     monkeypatch.chdir(tmp_path)
     p = config.Params(t=0.5, tstep=4, checkpoint=2, write_result=100)
     U_hat = np.ones((3, 4, 4, 3), complex)
-    f = NSFile(str(tmp_path / "run"))
+    f = NSFile(str(tmp_path / "run"), checkpoint={"data": {"0": {"U": [U_hat]}}})
     f.update(p, U_hat=U_hat)
     d = np.load(str(tmp_path / "run_c.npz"))
-    assert d["tstep"] == 4 and np.allclose(d["U_hat"], 1)
+    assert d["tstep"] == 4 and d["t"] == 0.5 and np.allclose(d["U/3D/0"], 1)
     open("killspectraldns", "w").close()
     p.tstep = 5
+    U_hat *= 2
     with pytest.raises(SystemExit):
-        f.update(p, U_hat=2 * U_hat)
-    assert np.allclose(np.load(str(tmp_path / "run_c.npz"))["U_hat"], 2)
+        f.update(p, U_hat=U_hat)
+    assert not os.path.exists("killspectraldns")
+    d = np.load(str(tmp_path / "run_c.npz"))
+    assert np.allclose(d["U/3D/0"], 2) and d["tstep"] == 5
+    assert not [q for q in os.listdir(tmp_path) if ".tmp" in q]
+
+
+def test_init_from_file(tmp_path):
+    """Restart: U_hat, t and tstep come back from the checkpoint (demo/Isotropic.py:267-282)."""
+    from spectraldns_gb300 import config
+    from spectraldns_gb300.config import AttributeDict
+    from spectraldns_gb300.h5io import HDF5File, init_from_file
+    rng = np.random.default_rng(0)
+    U_hat = rng.standard_normal((3, 8, 8, 5)) + 1j * rng.standard_normal((3, 8, 8, 5))
+    f = HDF5File(str(tmp_path / "NS"), checkpoint={"data": {"0": {"U": [U_hat]}}})
+    f.write_checkpoint(config.Params(t=0.25, tstep=7))
+    ctx = AttributeDict(U_hat=np.zeros_like(U_hat))
+    init_from_file(str(tmp_path / "NS"), None, ctx)
+    assert np.array_equal(ctx.U_hat, U_hat)
+    assert config.params.t == 0.25 and config.params.tstep == 7
+    with pytest.raises(ValueError):
+        init_from_file(str(tmp_path / "NS"), None, AttributeDict(U_hat=np.zeros((3, 4, 4, 3), complex)))
 
 
 def test_energy_fourier_shim():

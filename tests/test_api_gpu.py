@@ -90,5 +90,42 @@ def test_checkpoints_written(tmp_path, monkeypatch):
     solver, context = _run(["--M", "4", "4", "4", "--write_result", "2", "--checkpoint", "2", "NS"])
     d = np.load(str(tmp_path / "NS_c.npz"))
     assert int(d["tstep"]) == 10
-    assert np.allclose(d["U_hat"], context.U_hat)
-    assert (tmp_path / "NS_w_2.npz").exists()
+    assert np.allclose(d["U/3D/0"], context.U_hat)
+    w = np.load(str(tmp_path / "NS_w_2.npz"))
+    assert w["U/3D/2"].shape == (3, 16, 16, 16) and w["P/3D/2"].shape == (16, 16, 16)
+
+
+@pytest.mark.parametrize("precision,integrator", [("double", "RK4"), ("single", "RK4"), ("double", "BS5_fixed"),
+                                                  ("double", "ForwardEuler")])
+def test_restart_from_checkpoint(tmp_path, monkeypatch, precision, integrator):
+    """A run restarted from the checkpoint of step 5 ends where the uninterrupted run does (bit for bit)."""
+    import shutil
+    from spectraldns_gb300 import config, get_solver, solve
+    from spectraldns_gb300.h5io import init_from_file
+    monkeypatch.chdir(tmp_path)
+    args = ["--M", "5", "5", "5", "--precision", precision, "--integrator", integrator, "NS"]
+
+    def keep_step5(context):
+        # update() runs before the file hook: at step 6 NS_c.npz still holds step 5
+        if config.params.tstep == 6:
+            shutil.copy("NS_c.npz", "NS5_c.npz")
+
+    def run(restart=False):
+        config.update({"nu": 0.000625, "dt": 0.01, "T": 0.1, "convection": "Vortex"})
+        solver = get_solver(regression_test=lambda c: None, update=keep_step5, parse_args=args)
+        config.params.checkpoint = 5
+        context = solver.get_context()
+        initialize(solver, context)
+        if restart:
+            init_from_file("NS5", solver, context)
+            assert config.params.tstep == 5
+        solve(solver, context)
+        # 10 steps; in single precision dt is float32 (as the reference's Params return it) and
+        # the time loop may end with one more, tiny step to land on T
+        return context.U_hat.copy(), config.params.tstep
+
+    full, nfull = run()
+    assert int(np.load("NS5_c.npz")["tstep"]) == 5
+    restarted, nrest = run(restart=True)
+    assert nrest == nfull and nfull in (10, 11)
+    assert np.array_equal(restarted, full)

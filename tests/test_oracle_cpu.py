@@ -82,3 +82,43 @@ def test_isotropic_field_properties():
     assert np.abs(g.forward(g.backward(uh)) - uh).max() < 1e-12  # spectrum of a real field
     E = g.shell_spectrum(uh)
     assert 3 <= int(np.argmax(E)) <= 5  # k^4 exp(-2 (k/4)^2) peaks at k = 4
+
+
+@pytest.mark.parametrize("method,ntol", [("ForwardEuler", 4), ("AB2", 4), ("BS5_fixed", 7), ("BS5_adaptive", 7)])
+@pytest.mark.parametrize("N,L", [((16, 16, 16), (2 * np.pi,) * 3), ((64, 32, 16), (6 * np.pi, 4 * np.pi, 2 * np.pi))])
+def test_integrators_known_answers(method, ntol, N, L):
+    """tests/test_NSVV.py::test_integrators: TG to T = 0.1 meets tests/TG.py:125-126
+    to ntol digits (4 for ForwardEuler/AB2, 7 otherwise)."""
+    from oracle.ns_ref import Integrator
+    g = Grid(N, L)
+    uh = g.forward(taylor_green(g))
+    it = Integrator(g, method, tol=1e-6)
+    t, dt, tstep, T = 0.0, 0.01, 0, 0.1
+    while t + dt <= T + 1e-12:
+        uh, dt_next, took = it.step(uh, dt, tstep)
+        t += took
+        tstep += 1
+        dt = dt_next
+        if abs(t - T) < 1e-12:
+            break
+        if abs(t + dt - T) < 1e-12 or t + dt >= T + 1e-12:
+            dt = T - t
+    assert abs(t - T) < 1e-12
+    assert round(g.kinetic_energy(uh) - 0.124953117517, ntol) == 0
+    assert round(g.enstrophy(uh) - 0.375249930801, ntol) == 0
+
+
+def test_bs5_tableau_consistent():
+    """Row sums give the nodes; b and bhat are consistent (sum 1); FSAL: A[7] == b."""
+    from oracle.ns_ref import bs5_tableau
+    from spectraldns_gb300.integrators import _rows
+    A, b, bhat = bs5_tableau()
+    assert abs(b.sum() - 1) < 1e-15 and abs(bhat.sum() - 1) < 1e-15
+    assert np.array_equal(A[7], b)
+    c = A.sum(axis=1)
+    assert np.allclose(c, [0, 1 / 6, 2 / 9, 3 / 7, 2 / 3, 3 / 4, 1, 1], atol=1e-15)
+    # the GPU driver's tableau is the same table
+    Ag, bg, bhg = _rows(np.float64)
+    for i in range(8):
+        assert np.allclose(A[i, :i], Ag[i], rtol=0, atol=0)
+    assert np.allclose(b, bg, rtol=0, atol=0) and np.allclose(bhat, bhg, rtol=0, atol=0)
