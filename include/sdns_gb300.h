@@ -29,6 +29,10 @@
  *   sdns_set_source           the Source array added in ComputeRHS (NS.py:63, 259)
  *   sdns_diagnostics          demo/TG.py:97-103 and demo/Isotropic.py:167, 241-249 reductions
  *   sdns_spectrum             demo/Isotropic.py:88-114 (shell spectrum, bins k+0.5)
+ *   formulation SDNS_VV       spectralDNS/solvers/VV.py: the velocity-vorticity solver
+ *                             (get_context :23-38, Conv :85-103, add_linear :105-110,
+ *                             ComputeRHS :112-146); the context state is W_hat
+ *   sdns_velocity_vv          spectralDNS/solvers/VV.py:52-72 (compute_velocity / get_velocity)
  */
 #ifndef SDNS_GB300_H
 #define SDNS_GB300_H
@@ -53,6 +57,7 @@ enum sdns_status {
 enum sdns_precision { SDNS_SINGLE = 0, SDNS_DOUBLE = 1 };
 enum sdns_dealias { SDNS_DEALIAS_23 = 0, SDNS_DEALIAS_NONE = 1 };
 enum sdns_where { SDNS_HOST = 0, SDNS_DEVICE = 1 };
+enum sdns_formulation { SDNS_NS = 0, SDNS_VV = 1 };
 
 typedef struct sdns_ctx sdns_ctx;
 
@@ -65,11 +70,17 @@ typedef struct sdns_config {
   int32_t dealias;       /* SDNS_DEALIAS_23 (|k_i| < 2/3 (N_i/2+1)) or
                             SDNS_DEALIAS_NONE (Nyquist planes masked) */
   int32_t device;        /* CUDA device ordinal */
-  int32_t store_pressure;/* keep P_hat of the last RK4 stage for sdns_pressure */
-  int32_t reserved[4];
+  int32_t store_pressure;/* keep P_hat of the last RK4 stage for sdns_pressure (NS) */
+  int32_t formulation;   /* SDNS_NS (0): the state is the velocity U_hat and ComputeRHS
+                            is NS.py's; SDNS_VV: the state is the vorticity W_hat and
+                            ComputeRHS is VV.py's (i K x F(u x w) - nu K^2 W_hat + Source,
+                            u = F^-1(i K x W_hat / K^2)); no pressure, no forcing */
+  int32_t reserved[3];
 } sdns_config;
 
-/* diagnostics written by sdns_diagnostics (float64, full-spectrum sums) */
+/* diagnostics written by sdns_diagnostics (float64, full-spectrum sums).  For
+ * a SDNS_VV context the energy and divergence are those of the velocity
+ * i K x W_hat / K^2 and the enstrophy is 1/2 <w.w> of the state W_hat. */
 enum sdns_diag {
   SDNS_DIAG_ENERGY = 0,      /* 1/2 <u.u>              (demo/TG.py:98)  */
   SDNS_DIAG_ENSTROPHY = 1,   /* 1/2 <w.w>              (demo/TG.py:97)  */
@@ -119,6 +130,9 @@ int sdns_backward(sdns_ctx* ctx, const void* spec, void* phys, int32_t nfields, 
  * spectral vector u_hat (NULL: of the context state); pressure of the last
  * right-hand-side evaluation (needs store_pressure) */
 int sdns_velocity(sdns_ctx* ctx, void* u, int where);
+/* velocity F^-1(i K x w_hat / K^2) of a vorticity spectral vector w_hat (NULL:
+ * the context state, which is W_hat for a SDNS_VV context) */
+int sdns_velocity_vv(sdns_ctx* ctx, const void* w_hat, void* u, int where);
 int sdns_curl(sdns_ctx* ctx, const void* u_hat, void* curl, int where);
 int sdns_pressure(sdns_ctx* ctx, void* p, int where);
 int sdns_divergence(sdns_ctx* ctx, const void* u_hat, void* div, int where);

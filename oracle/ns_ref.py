@@ -18,6 +18,9 @@ What it restates (paths relative to the spectralDNS source tree):
 * ``spectralDNS/solvers/NS.py:219-261``  ComputeRHS (``rhs += Source``, :259).
 * ``spectralDNS/maths/integrators.py:149-159, 185-186``  classic RK4 with
   ``a=[1/6,1/3,1/3,1/6]``, ``b=[1/2,1/2,1]``.
+* ``spectralDNS/solvers/VV.py:52-67, 85-146`` the velocity-vorticity form:
+  ``u = F^-1(i K/K2 x w_hat)``, ``w = F^-1(w_hat)``,
+  ``rhs = i K x F(u x w) - nu K2 w_hat + Source`` (``compute_rhs_vv``).
 * ``spectralDNS/maths/integrators.py:15-147, 161-175, 193-233`` ForwardEuler,
   AB2 and the embedded Runge-Kutta step (FSAL, error norm "2", step-size
   controller) with the Bogacki-Shampine 5(4) tableau (``Integrator``).
@@ -165,14 +168,36 @@ class Grid:
             return rhs, dict(u=u, curl=w, nl=nl, P_hat=P)
         return rhs
 
-    def rk4_step(self, uh, dt, source=None):
-        """One classic RK4 step (integrators.py:149-159)."""
+    def velocity_of_vorticity(self, wh):
+        """compute_velocity's spectral part: i (K/K2) x w_hat (VV.py:52-67, cross2 with K_over_K2)."""
+        Q = self.K_over_K2
+        c = np.empty_like(wh)
+        c[0] = 1j * (Q[1] * wh[2] - Q[2] * wh[1])
+        c[1] = 1j * (Q[2] * wh[0] - Q[0] * wh[2])
+        c[2] = 1j * (Q[0] * wh[1] - Q[1] * wh[0])
+        return c
+
+    def compute_rhs_vv(self, wh, source=None):
+        """ComputeRHS of the velocity-vorticity form (VV.py:85-146), Vortex convection."""
+        m = self.mask
+        whm = wh * m
+        u = self.backward(self.velocity_of_vorticity(whm))
+        w = self.backward(whm)
+        v = self.forward(self.cross(u, w)) * m
+        rhs = self.curl_hat(v) - (self.nu * self.K2) * wh
+        if source is not None:
+            rhs += source
+        return rhs
+
+    def rk4_step(self, uh, dt, source=None, vv=False):
+        """One classic RK4 step (integrators.py:149-159) of the NS (or, vv, the VV) right-hand side."""
         u0 = uh.copy()
         u1 = uh.copy()
         u2 = uh.copy()
         dtc = np.asarray(dt, dtype=self.dtype)
+        F = self.compute_rhs_vv if vv else self.compute_rhs
         for rk in range(4):
-            rhs = self.compute_rhs(u0, source)
+            rhs = F(u0, source)
             if rk < 3:
                 u0 = u1 + np.asarray(RK4_B[rk], self.dtype) * dtc * rhs
             u2 += np.asarray(RK4_A[rk], self.dtype) * dtc * rhs

@@ -2,7 +2,7 @@
 
 Driver API with the interface of spectralDNS/__init__.py:19-123:
 ``get_solver(update, regression_test, additional_callback, mesh, parse_args)``
-returns the solver module selected by ``config.params.solver`` (``NS``), and
+returns the solver module selected by ``config.params.solver`` (``NS`` or ``VV``), and
 ``solve(solver, context)`` runs the time loop.  All compute runs in
 ``libsdns_gb300.so`` (see spectraldns_gb300.gpu).
 """
@@ -12,7 +12,7 @@ from . import config
 
 __version__ = "0.1.0"
 
-_SOLVERS = {"NS": "spectraldns_gb300.solvers.NS"}
+_SOLVERS = {"NS": "spectraldns_gb300.solvers.NS", "VV": "spectraldns_gb300.solvers.VV"}
 
 
 def get_solver(update=None, regression_test=None, additional_callback=None, mesh="triplyperiodic",

@@ -14,6 +14,7 @@ SDNS_OK, SDNS_EINVAL, SDNS_ECUDA, SDNS_ENOMEM, SDNS_ESTATE, SDNS_ENONFINITE = ra
 SDNS_SINGLE, SDNS_DOUBLE = 0, 1
 SDNS_DEALIAS_23, SDNS_DEALIAS_NONE = 0, 1
 SDNS_HOST, SDNS_DEVICE = 0, 1
+SDNS_NS, SDNS_VV = 0, 1
 DIAG_NAMES = ("energy", "enstrophy", "dissipation", "divergence", "cfl_rate", "time", "last_dt")
 SDNS_DIAG_COUNT = 8
 SDNS_LINCOMB_MAX = 8
@@ -28,7 +29,8 @@ class sdns_config(C.Structure):
         ("dealias", C.c_int32),
         ("device", C.c_int32),
         ("store_pressure", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("formulation", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
 
 
@@ -61,6 +63,7 @@ SIGNATURES = {
     "sdns_backward": (C.c_int, [_CTX, _P, _P, C.c_int32, C.c_int]),
     "sdns_velocity": (C.c_int, [_CTX, _P, C.c_int]),
     "sdns_curl": (C.c_int, [_CTX, _P, _P, C.c_int]),
+    "sdns_velocity_vv": (C.c_int, [_CTX, _P, _P, C.c_int]),
     "sdns_pressure": (C.c_int, [_CTX, _P, C.c_int]),
     "sdns_divergence": (C.c_int, [_CTX, _P, _P, C.c_int]),
     "sdns_diagnostics": (C.c_int, [_CTX, C.POINTER(C.c_double)]),

@@ -163,6 +163,7 @@ triplyperiodic.add_argument("--integrator", default="RK4",
                             choices=("RK4", "ForwardEuler", "AB2", "BS5_adaptive", "BS5_fixed"))
 _sub = triplyperiodic.add_subparsers(dest="solver")
 parser_NS = _sub.add_parser("NS", help="Navier-Stokes solver (Vortex form) on the GB300")
+parser_VV = _sub.add_parser("VV", help="Velocity-vorticity Navier-Stokes solver (Vortex form) on the GB300")
 
 solver = None  # set by get_solver
 

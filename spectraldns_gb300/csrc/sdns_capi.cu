@@ -70,6 +70,7 @@ struct sdns_ctx {
   sdns_config cfg;
   int dev = 0;
   bool dbl = false;
+  bool vv = false;           // velocity-vorticity formulation (state W_hat)
   size_t rsz = 4, csz = 8;  // real / complex element sizes of the working precision
   cudaStream_t st = nullptr;
   int N0, N1, N2, N2h;
@@ -279,7 +280,9 @@ __global__ void k_repitch(const C* in, C* out, long long rows, int pin, int pout
   }
 }
 
-// i K x u (curl) or i K . u (divergence) on the padded full layout
+// i K x u (mode 0, curl), i K . u (mode 1, divergence) or i K x u / K^2
+// (mode 2, the velocity of the vorticity u, spectralDNS/solvers/VV.py:52-67;
+// 0 at K = 0) on the padded full layout
 template <typename C>
 __global__ void k_curl_div(const C* u, C* out, Geo g, int div) {
   const long long n1 = (long long)g.N0 * g.N1 * g.Kzpf;
@@ -291,16 +294,18 @@ __global__ void k_curl_div(const C* u, C* out, Geo g, int div) {
     const double k0 = g.ks[0] * g.wave(p0, g.N0), k1 = g.ks[1] * g.wave(p1, g.N1), k2 = g.ks[2] * kz;
     const C a = u[i], b = u[n1 + i], c = u[2 * n1 + i];
     typedef decltype(a.x) R;
-    if (div) {
+    if (div == 1) {
       const double tr = k0 * a.x + k1 * b.x + k2 * c.x, ti = k0 * a.y + k1 * b.y + k2 * c.y;
       C o; o.x = (R)(-ti); o.y = (R)tr;
       out[i] = o;
     } else {
       double tr, ti;
       C o;
-      tr = k1 * c.x - k2 * b.x; ti = k1 * c.y - k2 * b.y; o.x = (R)(-ti); o.y = (R)tr; out[i] = o;
-      tr = k2 * a.x - k0 * c.x; ti = k2 * a.y - k0 * c.y; o.x = (R)(-ti); o.y = (R)tr; out[n1 + i] = o;
-      tr = k0 * b.x - k1 * a.x; ti = k0 * b.y - k1 * a.y; o.x = (R)(-ti); o.y = (R)tr; out[2 * n1 + i] = o;
+      const double K2 = k0 * k0 + k1 * k1 + k2 * k2;
+      const double s = div == 2 ? (K2 > 0.0 ? 1.0 / K2 : 0.0) : 1.0;
+      tr = s * (k1 * c.x - k2 * b.x); ti = s * (k1 * c.y - k2 * b.y); o.x = (R)(-ti); o.y = (R)tr; out[i] = o;
+      tr = s * (k2 * a.x - k0 * c.x); ti = s * (k2 * a.y - k0 * c.y); o.x = (R)(-ti); o.y = (R)tr; out[n1 + i] = o;
+      tr = s * (k0 * b.x - k1 * a.x); ti = s * (k0 * b.y - k1 * a.y); o.x = (R)(-ti); o.y = (R)tr; out[2 * n1 + i] = o;
     }
   }
 }
@@ -365,9 +370,33 @@ __global__ void k_step_end(const double* partials, long long nb, double* sc) {
 }
 
 // float64 sums over the compact state (+ outside modes in H): 1/2 sum |u|^2,
-// 1/2 sum |K x u|^2, 1/2 sum |K.u|^2
+// 1/2 sum |K x u|^2, 1/2 sum |K.u|^2.  vv: the state is the vorticity w and the
+// sums are 1/2 sum |u|^2, 1/2 sum |w|^2, 1/2 sum |K.u|^2 of u = i K x w / K^2.
+__device__ inline void diag_mode(double k0, double k1, double k2, double2 a, double2 b, double2 c, double w, bool vv,
+                                 double* s) {
+  const double xr = k1 * c.x - k2 * b.x, xi = k1 * c.y - k2 * b.y;
+  const double yr = k2 * a.x - k0 * c.x, yi = k2 * a.y - k0 * c.y;
+  const double zr = k0 * b.x - k1 * a.x, zi = k0 * b.y - k1 * a.y;
+  const double aa = a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y + c.x * c.x + c.y * c.y;
+  const double xx = xr * xr + xi * xi + yr * yr + yi * yi + zr * zr + zi * zi;
+  if (vv) {
+    const double K2 = k0 * k0 + k1 * k1 + k2 * k2;
+    const double iK2 = K2 > 0.0 ? 1.0 / K2 : 0.0;
+    s[0] += w * xx * iK2 * iK2;
+    s[1] += w * aa;
+    // u = i (K x w) / K^2: K . u = 0 up to rounding
+    const double dr = (k0 * xr + k1 * yr + k2 * zr) * iK2, di = (k0 * xi + k1 * yi + k2 * zi) * iK2;
+    s[2] += w * (dr * dr + di * di);
+  } else {
+    s[0] += w * aa;
+    s[1] += w * xx;
+    const double dr = k0 * a.x + k1 * b.x + k2 * c.x, di = k0 * a.y + k1 * b.y + k2 * c.y;
+    s[2] += w * (dr * dr + di * di);
+  }
+}
+
 template <typename C>
-__global__ void k_diag(const void* Sv, const C* H, Geo g, long long ncomp1, double* part) {
+__global__ void k_diag(const void* Sv, const C* H, Geo g, long long ncomp1, double* part, int vv) {
   using AC = Acc<decltype(C::x)>;
   const typename AC::T* S = reinterpret_cast<const typename AC::T*>(Sv);
   __shared__ double red[3][32];
@@ -380,13 +409,7 @@ __global__ void k_diag(const void* Sv, const C* H, Geo g, long long ncomp1, doub
     const double k0 = g.ks[0] * g.m0.wave(r0), k1 = g.ks[1] * g.m1.wave(r1), k2 = g.ks[2] * kz;
     const double2 a = AC::get(S, i), b = AC::get(S, ncomp1 + i), c = AC::get(S, 2 * ncomp1 + i);
     const double w = (kz == 0 || 2 * kz == 2 * (g.N2h - 1)) ? 0.5 : 1.0;
-    s[0] += w * (a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y + c.x * c.x + c.y * c.y);
-    const double xr = k1 * c.x - k2 * b.x, xi = k1 * c.y - k2 * b.y;
-    const double yr = k2 * a.x - k0 * c.x, yi = k2 * a.y - k0 * c.y;
-    const double zr = k0 * b.x - k1 * a.x, zi = k0 * b.y - k1 * a.y;
-    s[1] += w * (xr * xr + xi * xi + yr * yr + yi * yi + zr * zr + zi * zi);
-    const double dr = k0 * a.x + k1 * b.x + k2 * c.x, di = k0 * a.y + k1 * b.y + k2 * c.y;
-    s[2] += w * (dr * dr + di * di);
+    diag_mode(k0, k1, k2, a, b, c, w, vv != 0, s);
   }
   if (H) {
     const long long f1 = (long long)g.N0 * g.N1 * g.N2h;
@@ -397,14 +420,7 @@ __global__ void k_diag(const void* Sv, const C* H, Geo g, long long ncomp1, doub
       const double k0 = g.ks[0] * g.wave(p0, g.N0), k1 = g.ks[1] * g.wave(p1, g.N1), k2 = g.ks[2] * kz;
       const C a = H[i], b = H[f1 + i], c = H[2 * f1 + i];
       const double w = (kz == 0 || kz == g.N2h - 1) ? 0.5 : 1.0;
-      s[0] += w * ((double)a.x * a.x + (double)a.y * a.y + (double)b.x * b.x + (double)b.y * b.y + (double)c.x * c.x +
-                   (double)c.y * c.y);
-      const double xr = k1 * c.x - k2 * b.x, xi = k1 * c.y - k2 * b.y;
-      const double yr = k2 * a.x - k0 * c.x, yi = k2 * a.y - k0 * c.y;
-      const double zr = k0 * b.x - k1 * a.x, zi = k0 * b.y - k1 * a.y;
-      s[1] += w * (xr * xr + xi * xi + yr * yr + yi * yi + zr * zr + zi * zi);
-      const double dr = k0 * a.x + k1 * b.x + k2 * c.x, di = k0 * a.y + k1 * b.y + k2 * c.y;
-      s[2] += w * (dr * dr + di * di);
+      diag_mode(k0, k1, k2, make_double2(a.x, a.y), make_double2(b.x, b.y), make_double2(c.x, c.y), w, vv != 0, s);
     }
   }
   for (int q = 0; q < 3; ++q)
@@ -421,10 +437,20 @@ __global__ void k_diag(const void* Sv, const C* H, Geo g, long long ncomp1, doub
   }
 }
 
+// |u|^2 of one mode: the state itself, or (vv) the velocity i K x w / K^2 of the vorticity state
+__device__ inline double mode_u2(double k0, double k1, double k2, double2 a, double2 b, double2 c, int vv) {
+  if (!vv) return a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y + c.x * c.x + c.y * c.y;
+  const double xr = k1 * c.x - k2 * b.x, xi = k1 * c.y - k2 * b.y;
+  const double yr = k2 * a.x - k0 * c.x, yi = k2 * a.y - k0 * c.y;
+  const double zr = k0 * b.x - k1 * a.x, zi = k0 * b.y - k1 * a.y;
+  const double K2 = k0 * k0 + k1 * k1 + k2 * k2;
+  return K2 > 0.0 ? (xr * xr + xi * xi + yr * yr + yi * yi + zr * zr + zi * zi) / (K2 * K2) : 0.0;
+}
+
 // shell spectrum of demo/Isotropic.py:88-114: bin i collects i+0.5 < |K| <= i+1.5
 template <typename C>
 __global__ void k_spectrum(const void* Sv, const C* H, Geo g, long long ncomp1, double* sums, double* counts,
-                           int nb) {
+                           int nb, int vv) {
   using AC = Acc<decltype(C::x)>;
   const typename AC::T* S = reinterpret_cast<const typename AC::T*>(Sv);
   const long long n1 = (long long)g.m0.rows() * g.m1.rows() * g.Kzp;
@@ -438,7 +464,7 @@ __global__ void k_spectrum(const void* Sv, const C* H, Geo g, long long ncomp1, 
     if (b < 0 || b > nb - 2) continue;
     const double2 a = AC::get(S, i), bb = AC::get(S, ncomp1 + i), c = AC::get(S, 2 * ncomp1 + i);
     const double w = (kz == 0) ? 1.0 : 2.0;
-    atomicAdd(&sums[b], w * (a.x * a.x + a.y * a.y + bb.x * bb.x + bb.y * bb.y + c.x * c.x + c.y * c.y));
+    atomicAdd(&sums[b], w * mode_u2(k0, k1, k2, a, bb, c, vv));
   }
   // the reference averages over every mode of the (N0, N1, N2/2+1) array in the shell
   const long long f1c = (long long)g.N0 * g.N1 * g.N2h;
@@ -462,8 +488,8 @@ __global__ void k_spectrum(const void* Sv, const C* H, Geo g, long long ncomp1, 
       const C a = H[i], bb = H[f1 + i], c = H[2 * f1 + i];
       const double w = (kz == 0 || kz == g.N2h - 1) ? 1.0 : 2.0;
       if (!in)
-        atomicAdd(&sums[b], w * ((double)a.x * a.x + (double)a.y * a.y + (double)bb.x * bb.x + (double)bb.y * bb.y +
-                                 (double)c.x * c.x + (double)c.y * c.y));
+        atomicAdd(&sums[b], w * mode_u2(k0, k1, k2, make_double2(a.x, a.y), make_double2(bb.x, bb.y),
+                                        make_double2(c.x, c.y), vv));
     }
   }
 }
@@ -692,7 +718,7 @@ int launch_stage_sweeps(sdns_ctx* c, const void* yin, int stage, bool cfl_rate, 
   for (int i = 0; i < 3; ++i) a.kscale[i] = c->kscale[i];
   a.m1 = c->m1; a.Kzp = (int)Kzp;
   tstart(0);
-  CKL(c->dbl ? Kernels<double>::axis_curl_inv(a, s) : Kernels<float>::axis_curl_inv(a, s));
+  CKL(c->dbl ? Kernels<double>::axis_curl_inv(a, s, c->vv) : Kernels<float>::axis_curl_inv(a, s, c->vv));
   tstop(0);
   // y^-1: T1 -> T2 [6][N0][N1][Kzp]
   AxisArgs b = {};
@@ -757,6 +783,8 @@ int launch_stage_sweeps(sdns_ctx* c, const void* yin, int stage, bool cfl_rate, 
   r.force_alpha = (c->eps > 0 && stage < 4) ? c->sc + SC_ALPHA : nullptr;
   r.kf2 = c->kf * c->kf;
   r.partials = c->partials;
+  r.vv = c->vv ? 1 : 0;
+  if (c->vv) r.p_out = nullptr;
   tstart(5);
   CKL(c->dbl ? Kernels<double>::rk_update(r, s) : Kernels<float>::rk_update(r, s));
   tstop(5);
@@ -818,6 +846,8 @@ int sdns_create(const sdns_config* cfg, sdns_ctx** out) {
     return fail(SDNS_EINVAL, "precision must be SDNS_SINGLE or SDNS_DOUBLE");
   if (cfg->dealias != SDNS_DEALIAS_23 && cfg->dealias != SDNS_DEALIAS_NONE)
     return fail(SDNS_EINVAL, "dealias must be SDNS_DEALIAS_23 or SDNS_DEALIAS_NONE");
+  if (cfg->formulation != SDNS_NS && cfg->formulation != SDNS_VV)
+    return fail(SDNS_EINVAL, "formulation must be SDNS_NS or SDNS_VV");
   int ndev = 0;
   cudaError_t ce = cudaGetDeviceCount(&ndev);
   if (ce != cudaSuccess || ndev == 0) {
@@ -829,6 +859,7 @@ int sdns_create(const sdns_config* cfg, sdns_ctx** out) {
   c->cfg = *cfg;
   c->dev = cfg->device;
   c->dbl = cfg->precision == SDNS_DOUBLE;
+  c->vv = cfg->formulation == SDNS_VV;
   c->rsz = c->dbl ? 8 : 4;
   c->csz = 2 * c->rsz;
   c->N0 = cfg->n[0]; c->N1 = cfg->n[1]; c->N2 = cfg->n[2]; c->N2h = c->N2 / 2 + 1;
@@ -860,7 +891,7 @@ int sdns_create(const sdns_config* cfg, sdns_ctx** out) {
   if ((e = dalloc(c, &c->A, 3 * c->ncomp1 * 16))) return bail(e);
   if ((e = dalloc(c, &c->T1, 6LL * c->N0 * c->K1 * c->Kzp * cb))) return bail(e);
   if ((e = dalloc(c, &c->T2, 6LL * c->N0 * c->N1 * c->Kzp * cb))) return bail(e);
-  if (cfg->store_pressure && (e = dalloc(c, &c->Pc, c->ncomp1 * cb))) return bail(e);
+  if (cfg->store_pressure && !c->vv && (e = dalloc(c, &c->Pc, c->ncomp1 * cb))) return bail(e);
   if ((e = dalloc(c, &c->sc, SC_COUNT * 8))) return bail(e);
   if ((e = dalloc(c, &c->flag, 16))) return bail(e);
   // blocks of the pointwise RK update (one energy/enstrophy partial pair each)
@@ -1054,6 +1085,7 @@ int sdns_compute_rhs(sdns_ctx* c, const void* u_hat, void* rhs, int where) {
 int sdns_set_forcing(sdns_ctx* c, double eps, double kf) {
   int e = check_ctx(c);
   if (e) return e;
+  if (c->vv && eps > 0) return fail(SDNS_EINVAL, "the forcing is defined for the velocity formulation (SDNS_NS) only");
   c->eps = eps > 0 ? eps : 0;
   c->kf = kf;
   c->gkey = ~0ull;
@@ -1150,6 +1182,7 @@ int sdns_velocity(sdns_ctx* c, void* u, int where) {
   int e = check_ctx(c);
   if (e) return e;
   if (!c->has_state) return fail(SDNS_ESTATE, "no state set");
+  if (c->vv) return sdns_velocity_vv(c, nullptr, u, where);
   if ((e = ensure_full_bufs(c))) return e;
   if ((e = state_to_padded(c, c->F1))) return e;
   if ((e = full_backward(c, c->F1, c->F2, 3))) return e;
@@ -1168,15 +1201,32 @@ int spectral_to_padded(sdns_ctx* c, const void* u_hat, int where) {
   return repitch(c, c->stage, c->F2, 3, c->N2h, c->Kzpf, c->N2h);
 }
 
+// padded F2 (3 fields) -> F1 by k_curl_div in the given mode
+int curl_div_f2(sdns_ctx* c, int mode) {
+  Geo g = geo(c);
+  if (c->dbl) k_curl_div<double2><<<nblocks(c->npadf1), 256, 0, c->st>>>((const double2*)c->F2, (double2*)c->F1, g, mode);
+  else k_curl_div<float2><<<nblocks(c->npadf1), 256, 0, c->st>>>((const float2*)c->F2, (float2*)c->F1, g, mode);
+  CK(cudaGetLastError());
+  return SDNS_OK;
+}
+
+int sdns_velocity_vv(sdns_ctx* c, const void* w_hat, void* u, int where) {
+  int e = check_ctx(c);
+  if (e) return e;
+  if (!u) return fail(SDNS_EINVAL, "null output");
+  if ((e = ensure_full_bufs(c))) return e;
+  if ((e = spectral_to_padded(c, w_hat, where))) return e;
+  if ((e = curl_div_f2(c, 2))) return e;
+  if ((e = full_backward(c, c->F1, c->F2, 3))) return e;
+  return copy_out(c, u, c->PH, 3 * c->nphys1 * (long long)c->rsz, where);
+}
+
 int sdns_curl(sdns_ctx* c, const void* u_hat, void* w, int where) {
   int e = check_ctx(c);
   if (e) return e;
   if ((e = ensure_full_bufs(c))) return e;
   if ((e = spectral_to_padded(c, u_hat, where))) return e;
-  Geo g = geo(c);
-  if (c->dbl) k_curl_div<double2><<<nblocks(c->npadf1), 256, 0, c->st>>>((const double2*)c->F2, (double2*)c->F1, g, 0);
-  else k_curl_div<float2><<<nblocks(c->npadf1), 256, 0, c->st>>>((const float2*)c->F2, (float2*)c->F1, g, 0);
-  CK(cudaGetLastError());
+  if ((e = curl_div_f2(c, 0))) return e;
   if ((e = full_backward(c, c->F1, c->F2, 3))) return e;
   return copy_out(c, w, c->PH, 3 * c->nphys1 * (long long)c->rsz, where);
 }
@@ -1186,10 +1236,12 @@ int sdns_divergence(sdns_ctx* c, const void* u_hat, void* d, int where) {
   if (e) return e;
   if ((e = ensure_full_bufs(c))) return e;
   if ((e = spectral_to_padded(c, u_hat, where))) return e;
-  Geo g = geo(c);
-  if (c->dbl) k_curl_div<double2><<<nblocks(c->npadf1), 256, 0, c->st>>>((const double2*)c->F2, (double2*)c->F1, g, 1);
-  else k_curl_div<float2><<<nblocks(c->npadf1), 256, 0, c->st>>>((const float2*)c->F2, (float2*)c->F1, g, 1);
-  CK(cudaGetLastError());
+  if (c->vv && !u_hat) {
+    // divergence of the velocity of the state W_hat: F2 -> velocity F1 -> back into F2
+    if ((e = curl_div_f2(c, 2))) return e;
+    CK(cudaMemcpyAsync(c->F2, c->F1, 3 * c->npadf1 * (long long)c->csz, cudaMemcpyDeviceToDevice, c->st));
+  }
+  if ((e = curl_div_f2(c, 1))) return e;
   if ((e = full_backward(c, c->F1, c->F2, 1))) return e;
   return copy_out(c, d, c->PH, c->nphys1 * (long long)c->rsz, where);
 }
@@ -1197,6 +1249,7 @@ int sdns_divergence(sdns_ctx* c, const void* u_hat, void* d, int where) {
 int sdns_pressure(sdns_ctx* c, void* p, int where) {
   int e = check_ctx(c);
   if (e) return e;
+  if (c->vv) return fail(SDNS_EINVAL, "the velocity-vorticity formulation has no pressure (VV.py:27)");
   if (!c->Pc) return fail(SDNS_ESTATE, "pressure is not stored (create the context with store_pressure=1)");
   if ((e = ensure_full_bufs(c))) return e;
   Geo g = geo(c);
@@ -1220,8 +1273,10 @@ int sdns_diagnostics(sdns_ctx* c, double* out) {
   const unsigned nb = 152 * 4;
   double* part = nullptr;
   if ((e = dalloc(c, &part, 3LL * nb * 8))) return e;
-  if (c->dbl) k_diag<double2><<<nb, 256, 0, c->st>>>(c->S, c->high ? (const double2*)c->H : nullptr, g, c->ncomp1, part);
-  else k_diag<float2><<<nb, 256, 0, c->st>>>(c->S, c->high ? (const float2*)c->H : nullptr, g, c->ncomp1, part);
+  if (c->dbl)
+    k_diag<double2><<<nb, 256, 0, c->st>>>(c->S, c->high ? (const double2*)c->H : nullptr, g, c->ncomp1, part, c->vv);
+  else
+    k_diag<float2><<<nb, 256, 0, c->st>>>(c->S, c->high ? (const float2*)c->H : nullptr, g, c->ncomp1, part, c->vv);
   CK(cudaGetLastError());
   std::vector<double> h(3 * nb);
   double scal[SC_COUNT];
@@ -1256,10 +1311,10 @@ int sdns_spectrum(sdns_ctx* c, double* Ek, int32_t nbins) {
   Geo g = geo(c);
   if (c->dbl)
     k_spectrum<double2><<<152 * 4, 256, 0, c->st>>>(c->S, c->high ? (const double2*)c->H : nullptr, g, c->ncomp1, d,
-                                                   d + nbins, nbins);
+                                                   d + nbins, nbins, c->vv);
   else
     k_spectrum<float2><<<152 * 4, 256, 0, c->st>>>(c->S, c->high ? (const float2*)c->H : nullptr, g, c->ncomp1, d,
-                                                  d + nbins, nbins);
+                                                  d + nbins, nbins, c->vv);
   CK(cudaGetLastError());
   std::vector<double> h(2 * nbins);
   CK(cudaMemcpyAsync(h.data(), d, 2LL * nbins * 8, cudaMemcpyDeviceToHost, c->st));

@@ -103,6 +103,8 @@ struct RKArgs {
   const double* force_alpha; // optional device scalar; forcing on 0 < K2 <= kf2
   double kf2;
   double* partials;          // [gridDim.x][4] energy, enstrophy sums (stage 3)
+  int vv;                    // velocity-vorticity form: the state is W_hat and the
+                             // convective term is i K x (nonlinear term), no projection
 };
 
 // message returned by sdns_last_error() (thread-local)
@@ -110,7 +112,9 @@ void set_last_error(const char* msg);
 
 template <typename Real> struct Kernels {
   static int axis_plain(const AxisArgs& a, int sign, cudaStream_t s);
-  static int axis_curl_inv(const AxisArgs& a, cudaStream_t s);
+  // x^-1 sweep producing the six fields of the z sweep: NS (vv false) u_hat and
+  // i K x u_hat; VV (vv true) i K x w_hat / K^2 and w_hat
+  static int axis_curl_inv(const AxisArgs& a, cudaStream_t s, bool vv = false);
   static int zline_ns(const ZArgs& a, cudaStream_t s);
   static int zline_c2r(const ZArgs& a, cudaStream_t s);
   static int zline_r2c(const ZArgs& a, cudaStream_t s);

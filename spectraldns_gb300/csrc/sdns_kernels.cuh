@@ -186,12 +186,15 @@ __global__ void __launch_bounds__(256, axis_r32<Real, N>::value ? 2 : 3) k_axis_
 
 // x^-1 sweep with the curl: one block stages the three velocity components of
 // a tile of W lines once and produces all six output fields from them (u_hat
-// and i K x u_hat), one line transform per warp and field.
+// and i K x u_hat), one line transform per warp and field.  With VV the staged
+// vector is the vorticity w_hat and the six fields are the velocity
+// i K x w_hat / K^2 (spectralDNS/solvers/VV.py:52-67, K_over_K2 with K2 = 0 -> 1)
+// and w_hat itself (VV.py:97-98).
 __host__ __device__ inline int staged_rows(int rin, int W, int csz) {
   return tile_pitch((rin - 1) + ((rin - 1) >> 4) + 1, W, csz);
 }
 
-template <typename Real, int N>
+template <typename Real, int N, bool VV = false>
 __global__ void __launch_bounds__(512, 1) k_axis_curl6(AxisArgs a) {
   using C = typename cplx_of<Real>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -239,10 +242,15 @@ __global__ void __launch_bounds__(512, 1) k_axis_curl6(AxisArgs a) {
 #pragma unroll 1
   for (int f = 0; f < 6; ++f) {
     C* line = work + wl * LD;
-    int c1 = f, c2 = 0;
-    if (f == 3) { c1 = 2; c2 = 1; }       // i (k1 uz - kz uy)
-    else if (f == 4) { c1 = 0; c2 = 2; }  // i (kz ux - k0 uz)
-    else if (f == 5) { c1 = 1; c2 = 0; }  // i (k0 uy - k1 ux)
+    // cross-product field: NS fields 3..5, VV fields 0..2; cf = its component
+    const bool crossf = VV ? (f < 3) : (f >= 3);
+    const int cf = f < 3 ? f : f - 3;
+    int c1 = cf, c2 = 0;
+    if (crossf) {
+      if (cf == 0) { c1 = 2; c2 = 1; }       // i (k1 uz - kz uy)
+      else if (cf == 1) { c1 = 0; c2 = 2; }  // i (kz ux - k0 uz)
+      else { c1 = 1; c2 = 0; }               // i (k0 uy - k1 ux)
+    }
     const C* s1 = comp + (size_t)(c1 * W + wl) * PR;
     const C* s2 = comp + (size_t)(c2 * W + wl) * PR;
     auto ld = [&](int p) -> C {
@@ -252,15 +260,21 @@ __global__ void __launch_bounds__(512, 1) k_axis_curl6(AxisArgs a) {
         if (p > mi.kc) r = p - N + 2 * mi.kc + 1;
       }
       const C v1 = s1[padp(r)];
-      if (f < 3) return v1;
+      if (!crossf) return v1;
       const C v2 = s2[padp(r)];
       C t;
-      if (f == 3) {
+      if (cf == 0 && !VV) {
         t = mk<C>(k1 * v1.x - kz * v2.x, k1 * v1.y - kz * v2.y);
       } else {
         const Real k0 = ks0 * (Real)mi.wave(r);
-        if (f == 4) t = mk<C>(kz * v1.x - k0 * v2.x, kz * v1.y - k0 * v2.y);
+        if (cf == 0) t = mk<C>(k1 * v1.x - kz * v2.x, k1 * v1.y - kz * v2.y);
+        else if (cf == 1) t = mk<C>(kz * v1.x - k0 * v2.x, kz * v1.y - k0 * v2.y);
         else t = mk<C>(k0 * v1.x - k1 * v2.x, k0 * v1.y - k1 * v2.y);
+        if constexpr (VV) {
+          const Real K2 = k0 * k0 + k1 * k1 + kz * kz;
+          const Real iK2 = K2 > (Real)0 ? (Real)1 / K2 : (Real)0;
+          t = mk<C>(t.x * iK2, t.y * iK2);
+        }
       }
       return mk<C>(-t.y, t.x);
     };
@@ -852,7 +866,7 @@ __device__ __forceinline__ double block_sum2(double x, double y, double* red, do
   return xs;
 }
 
-template <typename Real>
+template <typename Real, bool VV = false>
 __global__ void __launch_bounds__(256) k_rk_update(RKArgs a) {
   using C = typename cplx_of<Real>::type;
   using AT = typename Acc<Real>::T;
@@ -918,9 +932,14 @@ __global__ void __launch_bounds__(256) k_rk_update(RKArgs a) {
         if (src) qv[c] = src[oc];
       }
       const Real iK2 = K2 > (Real)0 ? (Real)1 / K2 : (Real)0;
-      const C P = mk<C>((nlv[0].x * k[0] + nlv[1].x * k[1] + nlv[2].x * k[2]) * iK2,
-                        (nlv[0].y * k[0] + nlv[1].y * k[1] + nlv[2].y * k[2]) * iK2);
-      if (a.p_out) reinterpret_cast<C*>(a.p_out)[o] = P;
+      // convective term: NS projects the nonlinear term (NS.py:203-212), VV
+      // takes its curl i K x nl (VV.py:103), component by component below
+      C P = czero<C>();
+      if constexpr (!VV) {
+        P = mk<C>((nlv[0].x * k[0] + nlv[1].x * k[1] + nlv[2].x * k[2]) * iK2,
+                  (nlv[0].y * k[0] + nlv[1].y * k[1] + nlv[2].y * k[2]) * iK2);
+        if (a.p_out) reinterpret_cast<C*>(a.p_out)[o] = P;
+      }
       const Real nuK2 = (Real)a.nu * K2;
       Real snx[3] = {0, 0, 0}, sny[3] = {0, 0, 0};
 #pragma unroll
@@ -929,7 +948,14 @@ __global__ void __launch_bounds__(256) k_rk_update(RKArgs a) {
         const AT s = sv[c];
         AT acc = av[c];
         const C u = stage == 0 ? mk<C>((Real)s.x, (Real)s.y) : uv[c];
-        C rhs = mk<C>(nlv[c].x - P.x * k[c] - nuK2 * u.x, nlv[c].y - P.y * k[c] - nuK2 * u.y);
+        C rhs;
+        if constexpr (VV) {
+          const int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+          rhs = mk<C>(-(k[c1] * nlv[c2].y - k[c2] * nlv[c1].y) - nuK2 * u.x,
+                      (k[c1] * nlv[c2].x - k[c2] * nlv[c1].x) - nuK2 * u.y);
+        } else {
+          rhs = mk<C>(nlv[c].x - P.x * k[c] - nuK2 * u.x, nlv[c].y - P.y * k[c] - nuK2 * u.y);
+        }
         if (src) { rhs.x += (Real)qv[c].x; rhs.y += (Real)qv[c].y; }
         if (forced) { rhs.x += alph * (Real)s.x; rhs.y += alph * (Real)s.y; }
         if (stage == 4) {
@@ -979,8 +1005,13 @@ __global__ void __launch_bounds__(256) k_rk_update(RKArgs a) {
         const Real cyr = k[2] * snx[0] - k[0] * snx[2], cyi = k[2] * sny[0] - k[0] * sny[2];
         const Real czr = k[0] * snx[1] - k[1] * snx[0], czi = k[0] * sny[1] - k[1] * sny[0];
         const Real z = cxr * cxr + cxi * cxi + cyr * cyr + cyi * cyi + czr * czr + czi * czi;
-        e_sum = wz * e;
-        z_sum = wz * z;
+        if constexpr (VV) {  // state w_hat: energy of i K x w_hat / K^2, enstrophy of w_hat
+          e_sum = wz * z * iK2 * iK2;
+          z_sum = wz * e;
+        } else {
+          e_sum = wz * e;
+          z_sum = wz * z;
+        }
       }
     }
   }
@@ -1057,7 +1088,7 @@ int Kernels<Real>::axis_plain(const AxisArgs& a, int sign, cudaStream_t s) {
 }
 
 template <typename Real, int N>
-static int launch_curl6(const AxisArgs& a, cudaStream_t s) {
+static int launch_curl6(const AxisArgs& a, cudaStream_t s, bool vv) {
   using C = typename cplx_of<Real>::type;
   // the x sweep reads lines l at in + c*in_fs + l (one run of lines per field)
   if (a.B != a.nlines || a.in_ss != 0 || a.out_ss != 0 || a.nfield != 6 || (a.out_rs & 1)) return (int)cudaErrorInvalidValue;
@@ -1070,20 +1101,21 @@ static int launch_curl6(const AxisArgs& a, cudaStream_t s) {
   int W = 512 / G;  // 16-line tiles at N = 512 (128-byte rows), halved while they do not fit
   while (W > 2 && bytes(W) > lim) W >>= 1;
   const size_t sm = bytes(W);
-  k_axis_curl6<Real, N><<<(unsigned)((a.nlines + W - 1) / W), W * G, sm, s>>>(a);
+  if (vv) k_axis_curl6<Real, N, true><<<(unsigned)((a.nlines + W - 1) / W), W * G, sm, s>>>(a);
+  else k_axis_curl6<Real, N, false><<<(unsigned)((a.nlines + W - 1) / W), W * G, sm, s>>>(a);
   return (int)cudaGetLastError();
 }
 
 template <typename Real>
-int Kernels<Real>::axis_curl_inv(const AxisArgs& a, cudaStream_t s) {
+int Kernels<Real>::axis_curl_inv(const AxisArgs& a, cudaStream_t s, bool vv) {
   switch (a.min.n) {
-    case 16: return launch_curl6<Real, 16>(a, s);
-    case 32: return launch_curl6<Real, 32>(a, s);
-    case 64: return launch_curl6<Real, 64>(a, s);
-    case 128: return launch_curl6<Real, 128>(a, s);
-    case 256: return launch_curl6<Real, 256>(a, s);
-    case 512: return launch_curl6<Real, 512>(a, s);
-    case 1024: return launch_curl6<Real, 1024>(a, s);
+    case 16: return launch_curl6<Real, 16>(a, s, vv);
+    case 32: return launch_curl6<Real, 32>(a, s, vv);
+    case 64: return launch_curl6<Real, 64>(a, s, vv);
+    case 128: return launch_curl6<Real, 128>(a, s, vv);
+    case 256: return launch_curl6<Real, 256>(a, s, vv);
+    case 512: return launch_curl6<Real, 512>(a, s, vv);
+    case 1024: return launch_curl6<Real, 1024>(a, s, vv);
     default: return (int)cudaErrorInvalidValue;
   }
 }
@@ -1091,7 +1123,8 @@ int Kernels<Real>::axis_curl_inv(const AxisArgs& a, cudaStream_t s) {
 template <typename Real>
 int Kernels<Real>::rk_update(const RKArgs& a, cudaStream_t s) {
   const dim3 grid((unsigned)((a.nlines + 255) / 256), (unsigned)a.m0.rows());
-  k_rk_update<Real><<<grid, 256, 0, s>>>(a);
+  if (a.vv) k_rk_update<Real, true><<<grid, 256, 0, s>>>(a);
+  else k_rk_update<Real, false><<<grid, 256, 0, s>>>(a);
   return (int)cudaGetLastError();
 }
 
@@ -1213,7 +1246,8 @@ int Kernels<Real>::smem_optin(int dev) {
   int mx = 0;
   cudaError_t e = cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
 #define SDNS_OPT(k) if (e == cudaSuccess) e = optin_one(k, mx)
-#define SDNS_OPT_N(n) SDNS_OPT((k_axis_p<Real, n, -1>)); SDNS_OPT((k_axis_p<Real, n, 1>)); SDNS_OPT((k_axis_curl6<Real, n>))
+#define SDNS_OPT_N(n) SDNS_OPT((k_axis_p<Real, n, -1>)); SDNS_OPT((k_axis_p<Real, n, 1>)); \
+  SDNS_OPT((k_axis_curl6<Real, n, false>)); SDNS_OPT((k_axis_curl6<Real, n, true>))
   SDNS_OPT_N(16); SDNS_OPT_N(32); SDNS_OPT_N(64); SDNS_OPT_N(128); SDNS_OPT_N(256); SDNS_OPT_N(512); SDNS_OPT_N(1024);
 #undef SDNS_OPT_N
   SDNS_OPT((k_zline_ns<Real, 16>)); SDNS_OPT((k_zline_ns<Real, 32>));

@@ -30,7 +30,7 @@ class Context:
     """GPU state of the NS solver (spectralDNS solvers/NS.py:12-72 get_context)."""
 
     def __init__(self, N, L=(2 * np.pi,) * 3, nu=0.000625, precision="double", dealias="2/3-rule",
-                 device=0, store_pressure=False):
+                 device=0, store_pressure=False, formulation="NS"):
         self.N = tuple(int(n) for n in N)
         self.L = tuple(float(x) for x in L)
         self.nu = float(nu)
@@ -38,8 +38,11 @@ class Context:
             raise ValueError("precision must be 'single' or 'double'")
         if dealias not in ("2/3-rule", "None"):
             raise ValueError("dealias %r is not supported by the GPU backend (2/3-rule or None)" % (dealias,))
+        if formulation not in ("NS", "VV"):
+            raise ValueError("formulation must be 'NS' (velocity) or 'VV' (velocity-vorticity)")
         self.precision = precision
         self.dealias = dealias
+        self.formulation = formulation
         self.device = int(device)
         self.real = np.float32 if precision == "single" else np.float64
         self.complex = np.complex64 if precision == "single" else np.complex128
@@ -53,7 +56,8 @@ class Context:
         cfg.precision = _lib.SDNS_SINGLE if precision == "single" else _lib.SDNS_DOUBLE
         cfg.dealias = _lib.SDNS_DEALIAS_23 if dealias == "2/3-rule" else _lib.SDNS_DEALIAS_NONE
         cfg.device = self.device
-        cfg.store_pressure = 1 if store_pressure else 0
+        cfg.store_pressure = 1 if store_pressure and formulation == "NS" else 0
+        cfg.formulation = _lib.SDNS_VV if formulation == "VV" else _lib.SDNS_NS
         self._L = _lib.lib()
         h = C.c_void_p()
         check(self._L.sdns_create(C.byref(cfg), C.byref(h)))
@@ -207,7 +211,12 @@ class Context:
         return self._finish(arr, wb, w)
 
     def velocity(self, out=None):
+        """Velocity of the context state (for a VV context: of the vorticity state)."""
         return self._phys(self._L.sdns_velocity, out, 3)
+
+    def velocity_vv(self, w_hat=None, out=None):
+        """F^-1(i K x w_hat / K^2): the velocity of a vorticity spectral vector (None: the state)."""
+        return self._phys_of(self._L.sdns_velocity_vv, w_hat, out, 3)
 
     def _phys_of(self, fn, u_hat, out, nf):
         """fn(ctx, u_hat or NULL, out, where) for the spectral vector u_hat (None: the state)."""

@@ -85,6 +85,9 @@ def conv(*args):
     raise NotImplementedError
 
 
+_default_regression_test, _default_update, _default_additional_callback = regression_test, update, additional_callback
+
+
 def set_source(Source, **context):
     Source[:] = 0
     return Source
@@ -172,8 +175,12 @@ class _Work(dict):
 
 
 # ---------------------------------------------------------------- context
-def get_context():
-    """Set up the GPU solver and the host arrays of NS.py:12-72."""
+def get_context(formulation="NS"):
+    """Set up the GPU solver and the host arrays of NS.py:12-72.
+
+    ``formulation="VV"`` makes the GPU context hold the vorticity (the
+    velocity-vorticity solver, spectraldns_gb300.solvers.VV, builds on this).
+    """
     float_, complex_, mpitype = datatypes(params.precision)
     if params.dealias == "3/2-rule":
         raise ValueError("the GB300 backend implements the 2/3 rule (and 'None'); the 3/2 rule is not supported")
@@ -185,7 +192,8 @@ def get_context():
     L = tuple(float(x) for x in params.L)
     gpu = Context(N, L, nu=float(params.nu), precision=params.precision,
                   dealias="2/3-rule" if params.dealias == "2/3-rule" else "None",
-                  device=int(params.get("device", 0)), store_pressure=True)
+                  device=int(params.get("device", 0)), store_pressure=formulation == "NS",
+                  formulation=formulation)
     T = Space(gpu, 1)
     VT = Space(gpu, 3)
     Tp, VTp = T, VT

@@ -1,1 +1,1 @@
-"""Solver modules of the GB300 backend (only NS)."""
+"""Solver modules of the GB300 backend: NS (velocity) and VV (velocity-vorticity)."""

@@ -122,3 +122,19 @@ def test_bs5_tableau_consistent():
     for i in range(8):
         assert np.allclose(A[i, :i], Ag[i], rtol=0, atol=0)
     assert np.allclose(b, bg, rtol=0, atol=0) and np.allclose(bhat, bhg, rtol=0, atol=0)
+
+
+@pytest.mark.parametrize("N,L", [((16, 16, 16), (2 * np.pi,) * 3), ((64, 32, 16), (6 * np.pi, 4 * np.pi, 2 * np.pi))])
+def test_vv_known_answers(N, L):
+    """tests/test_NSVV.py runs the VV solver on TG (initialize2: W_hat = i K x U_hat) against
+    tests/TG.py:125-126; the VV state stays the curl of the NS state."""
+    g = Grid(N, L)
+    uh = g.forward(taylor_green(g))
+    wh = g.curl_hat(uh)
+    for _ in range(10):
+        wh = g.rk4_step(wh, 0.01, vv=True)
+        uh = g.rk4_step(uh, 0.01)
+    U = g.backward(g.velocity_of_vorticity(wh))
+    assert round(0.5 * g.mean_square(U) - 0.124953117517, 7) == 0
+    assert round(0.5 * g.mean_square(g.backward(wh)) - 0.375249930801, 7) == 0
+    assert np.max(np.abs(wh - g.curl_hat(uh))) < 1e-13
