@@ -55,7 +55,7 @@ enum sdns_status {
 };
 
 enum sdns_precision { SDNS_SINGLE = 0, SDNS_DOUBLE = 1 };
-enum sdns_dealias { SDNS_DEALIAS_23 = 0, SDNS_DEALIAS_NONE = 1 };
+enum sdns_dealias { SDNS_DEALIAS_23 = 0, SDNS_DEALIAS_NONE = 1, SDNS_DEALIAS_32 = 2 };
 enum sdns_where { SDNS_HOST = 0, SDNS_DEVICE = 1 };
 enum sdns_formulation { SDNS_NS = 0, SDNS_VV = 1 };
 
@@ -67,8 +67,13 @@ typedef struct sdns_config {
   double nu;             /* viscosity */
   int32_t precision;     /* SDNS_SINGLE: FP32 transforms, FP64 RK4 accumulators;
                             SDNS_DOUBLE: everything FP64 */
-  int32_t dealias;       /* SDNS_DEALIAS_23 (|k_i| < 2/3 (N_i/2+1)) or
-                            SDNS_DEALIAS_NONE (Nyquist planes masked) */
+  int32_t dealias;       /* SDNS_DEALIAS_23 (|k_i| < 2/3 (N_i/2+1)),
+                            SDNS_DEALIAS_NONE (Nyquist planes masked) or
+                            SDNS_DEALIAS_32: the 3/2 rule (NS.py:29-31 with
+                            padding_factor 1.5): the nonlinear term is formed
+                            on a 3N/2 grid from all modes but the Nyquist ones
+                            and truncated back; fixed dt only (no CFL, no
+                            forcing), RK4 steps in the working precision */
   int32_t device;        /* CUDA device ordinal */
   int32_t store_pressure;/* keep P_hat of the last RK4 stage for sdns_pressure (NS) */
   int32_t formulation;   /* SDNS_NS (0): the state is the velocity U_hat and ComputeRHS

@@ -34,6 +34,13 @@ What it restates (paths relative to the spectralDNS source tree):
   backward unnormalised.  In-tree evidence: ``demo/TG.py:98-109`` (Parseval
   check ``energy_fourier(U_hat)/2 - 1/2<U^2> ~ 0``) and
   ``demo/Isotropic.py:67-69``.
+* ``spectralDNS/solvers/NS.py:29-31`` with ``padding_factor=1.5`` (the 3/2
+  rule): every mode but the Nyquist ones is transformed on a grid of 3N/2
+  points per axis (zero padded, unnormalised backward, forward scaled by
+  1/prod(3N/2)), the nonlinear term is truncated back to the N modes and
+  its Nyquist modes masked (``Grid(dealias="3/2-rule")``).  shenfun's own
+  padding (its Nyquist split) is third party and absent: that detail is
+  parity unpinned; the Nyquist modes are left out on input.
 * Diagnostics: ``demo/TG.py:97-103, 116-126`` (float64 mean-square
   reductions), ``demo/Isotropic.py:88-147`` (shell spectrum).
 
@@ -77,7 +84,7 @@ def dealias_cutoff(n: int, rule: str = "2/3-rule") -> int:
         while kc >= kmax:
             kc -= 1
         return kc
-    if rule in ("None", None):
+    if rule in ("None", None, "3/2-rule"):
         return n // 2 - 1
     raise ValueError("unsupported dealias rule %r" % (rule,))
 
@@ -115,6 +122,8 @@ class Grid:
         m1 = np.abs(self.ki[1]) <= self.kc[1]
         m2 = np.abs(self.ki[2]) <= self.kc[2]
         self.mask = (m0[:, None, None] & m1[None, :, None] & m2[None, None, :])
+        self.pad = dealias == "3/2-rule"
+        self.M = tuple(3 * n // 2 for n in self.N)
         # the physical mesh (NS.py:37 via shenfun local_mesh)
         self.X = [(np.arange(self.N[i]) * self.L[i] / self.N[i]) for i in range(3)]
 
@@ -130,6 +139,44 @@ class Grid:
         kw = {"workers": self.workers} if _HAVE_SCIPY else {}
         out = _fft.irfftn(uh, s=self.N, axes=(-3, -2, -1), **kw) * float(np.prod(self.N))
         return out.astype(self.dtype, copy=False)
+
+    def _pad_index(self):
+        """(source, target) index arrays of the N modes (Nyquist left out) in the padded spectrum."""
+        n0, n1, n2 = self.N
+        M0, M1, _ = self.M
+        i0 = np.r_[0:n0 // 2, n0 // 2 + 1:n0]
+        t0 = np.r_[0:n0 // 2, M0 - n0 // 2 + 1:M0]
+        i1 = np.r_[0:n1 // 2, n1 // 2 + 1:n1]
+        t1 = np.r_[0:n1 // 2, M1 - n1 // 2 + 1:M1]
+        i2 = np.arange(n2 // 2)
+        return (i0[:, None, None], i1[None, :, None], i2[None, None, :]), \
+            (t0[:, None, None], t1[None, :, None], i2[None, None, :])
+
+    def padded_backward(self, uh):
+        """Backward transform on the 3N/2 grid (zero padded spectrum, unnormalised)."""
+        src, dst = self._pad_index()
+        M0, M1, M2 = self.M
+        U = np.zeros(uh.shape[:-3] + (M0, M1, M2 // 2 + 1), dtype=np.complex128)
+        U[(Ellipsis,) + dst] = uh[(Ellipsis,) + src]
+        kw = {"workers": self.workers} if _HAVE_SCIPY else {}
+        out = _fft.irfftn(U, s=self.M, axes=(-3, -2, -1), **kw) * float(np.prod(self.M))
+        return out.astype(self.dtype, copy=False)
+
+    def padded_forward(self, u):
+        """Forward transform on the 3N/2 grid (scaled by 1/prod(3N/2)), truncated to the N modes."""
+        src, dst = self._pad_index()
+        kw = {"workers": self.workers} if _HAVE_SCIPY else {}
+        F = _fft.rfftn(u, axes=(-3, -2, -1), **kw) / float(np.prod(self.M))
+        out = np.zeros(u.shape[:-3] + self.spec_shape, dtype=self.cdtype)
+        out[(Ellipsis,) + src] = F[(Ellipsis,) + dst]
+        return out
+
+    def _nonlinear(self, a, b):
+        """F(F^-1(a) x F^-1(b)), masked: dealiased by truncation (2/3) or by padding (3/2)."""
+        m = self.mask
+        if self.pad:
+            return self.padded_forward(self.cross(self.padded_backward(a * m), self.padded_backward(b * m))) * m
+        return self.forward(self.cross(self.backward(a * m), self.backward(b * m))) * m
 
     # --- pieces of ComputeRHS --------------------------------------------
     def curl_hat(self, uh):
@@ -154,9 +201,14 @@ class Grid:
         """ComputeRHS for the Vortex form (NS.py:219-261)."""
         m = self.mask
         uhm = uh * m
-        u = self.backward(uhm)
-        w = self.backward(self.curl_hat(uhm))
-        nl = self.forward(self.cross(u, w)) * m
+        if self.pad:
+            u = self.padded_backward(uhm)
+            w = self.padded_backward(self.curl_hat(uhm))
+            nl = self.padded_forward(self.cross(u, w)) * m
+        else:
+            u = self.backward(uhm)
+            w = self.backward(self.curl_hat(uhm))
+            nl = self.forward(self.cross(u, w)) * m
         P = nl[0] * self.K_over_K2[0] + nl[1] * self.K_over_K2[1] + nl[2] * self.K_over_K2[2]
         rhs = np.empty_like(uh)
         nuK2 = self.nu * self.K2
@@ -181,9 +233,7 @@ class Grid:
         """ComputeRHS of the velocity-vorticity form (VV.py:85-146), Vortex convection."""
         m = self.mask
         whm = wh * m
-        u = self.backward(self.velocity_of_vorticity(whm))
-        w = self.backward(whm)
-        v = self.forward(self.cross(u, w)) * m
+        v = self._nonlinear(self.velocity_of_vorticity(whm), whm)
         rhs = self.curl_hat(v) - (self.nu * self.K2) * wh
         if source is not None:
             rhs += source

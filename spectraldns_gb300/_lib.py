@@ -12,7 +12,7 @@ from . import build as _build
 
 SDNS_OK, SDNS_EINVAL, SDNS_ECUDA, SDNS_ENOMEM, SDNS_ESTATE, SDNS_ENONFINITE = range(6)
 SDNS_SINGLE, SDNS_DOUBLE = 0, 1
-SDNS_DEALIAS_23, SDNS_DEALIAS_NONE = 0, 1
+SDNS_DEALIAS_23, SDNS_DEALIAS_NONE, SDNS_DEALIAS_32 = 0, 1, 2
 SDNS_HOST, SDNS_DEVICE = 0, 1
 SDNS_NS, SDNS_VV = 0, 1
 DIAG_NAMES = ("energy", "enstrophy", "dissipation", "divergence", "cfl_rate", "time", "last_dt")

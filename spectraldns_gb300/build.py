@@ -26,6 +26,7 @@ SOURCES = [
     "sdns_capi.cu",
     "sdns_noalloc.cu",
     "sdns_les.cu",
+    "sdns_pad32.cu",
 ]
 EXTRA_SOURCES: list = []  # appended by later modules (LES closure kernels)
 

@@ -105,6 +105,18 @@ struct sdns_ctx {
   long long nblk_rk = 0;
   int* flag = nullptr;
   double* red = nullptr;     // per-block partial sums of sdns_error_norm
+  // 3/2-rule contexts: caller-layout state and RK4 vectors, padded scratch
+  bool pad32 = false;
+  int M[3] = {0, 0, 0};
+  void* U32 = nullptr;       // state [3][N0][N1][N2h]
+  void* U32a = nullptr;      // RK4 u1
+  void* U32b = nullptr;      // RK4 u2
+  void* R32 = nullptr;       // rhs
+  void* P32 = nullptr;       // P_hat of the last rhs (store_pressure)
+  void* spec32 = nullptr;    // [6][M0][M1][M2h]
+  void* phys32 = nullptr;    // [6][M0][M1][M2]
+  void* tw32 = nullptr;      // W_{M_i}^j tables, one per axis
+  long long twoff32[3] = {0, 0, 0};
   // host state
   double eps = 0, kf = 0, cfl = 0, last_dt = -1;
   bool has_state = false;
@@ -570,6 +582,16 @@ Geo geo(const sdns_ctx* c) {
   return g;
 }
 
+// geometry and caller-layout array of the float64 reductions: the compact
+// state plus the modes outside it (H), or, for a 3/2-rule context, the whole
+// caller-layout state as "outside" modes of an empty compact set
+Geo diag_geo(const sdns_ctx* c) {
+  Geo g = geo(c);
+  if (c->pad32) { g.Kz = 0; g.Kzp = 0; }
+  return g;
+}
+const void* diag_full(const sdns_ctx* c) { return c->pad32 ? c->U32 : (c->high ? c->H : nullptr); }
+
 inline unsigned nblocks(long long n, int bs = 256) {
   long long b = (n + bs - 1) / bs;
   if (b > 152LL * 32) b = 152LL * 32;
@@ -677,8 +699,10 @@ int repitch(sdns_ctx* c, const void* in, void* out, int nf, int pin, int pout, i
   return c->dbl ? repitch<double2>(c, in, out, nf, pin, pout, ncopy) : repitch<float2>(c, in, out, nf, pin, pout, ncopy);
 }
 
-// compact FP64 state (+H) -> padded full F (3 fields)
+// compact FP64 state (+H) -> padded full F (3 fields); a 3/2-rule context's
+// state is already in the caller layout
 int state_to_padded(sdns_ctx* c, void* F) {
+  if (c->pad32) return repitch(c, c->U32, F, 3, c->N2h, c->Kzpf, c->N2h);
   Geo g = geo(c);
   if (c->dbl)
     k_scatter<double2><<<nblocks(3 * c->npadf1), 256, 0, c->st>>>(
@@ -686,6 +710,67 @@ int state_to_padded(sdns_ctx* c, void* F) {
   else
     k_scatter<float2><<<nblocks(3 * c->npadf1), 256, 0, c->st>>>(
         c->S, 1, (float2*)F, c->high ? (const float2*)c->H : nullptr, g, 3, c->Kzpf, c->ncomp1, 0);
+  CK(cudaGetLastError());
+  return SDNS_OK;
+}
+
+// ---- 3/2-rule contexts -------------------------------------------------------
+Pad32 pad32_of(const sdns_ctx* c) {
+  Pad32 p;
+  for (int i = 0; i < 3; ++i) {
+    p.N[i] = c->cfg.n[i];
+    p.M[i] = c->M[i];
+    p.ks[i] = c->kscale[i];
+    p.tw[i] = (const char*)c->tw32 + c->twoff32[i] * c->csz;
+  }
+  p.nu = c->cfg.nu;
+  p.dbl = c->dbl;
+  p.vv = c->vv;
+  p.spec = c->spec32;
+  p.phys = c->phys32;
+  return p;
+}
+
+int rhs32(sdns_ctx* c, const void* u, void* rhs, bool store_p) {
+  CKL(pad32_rhs(pad32_of(c), u, c->src_full, rhs, store_p ? c->P32 : nullptr, c->st));
+  return SDNS_OK;
+}
+
+__global__ void k_time_step(double* sc) { sc[SC_TIME] += sc[SC_DT]; }
+
+// out = base + sum c_k t_k on caller-layout vectors (the lincomb kernel)
+int lincomb_full(sdns_ctx* c, void* out, const void* base, int n, const double* coef, void* const* terms) {
+  LinTerms lt = {};
+  lt.n = n;
+  for (int k = 0; k < n; ++k) { lt.t[k] = terms[k]; lt.c[k] = coef[k]; }
+  const long long cnt = 3 * c->nfull1;
+  if (c->dbl) k_lincomb<double2><<<nblocks(cnt), 256, 0, c->st>>>((double2*)out, (const double2*)base, lt, cnt);
+  else k_lincomb<float2><<<nblocks(cnt), 256, 0, c->st>>>((float2*)out, (const float2*)base, lt, cnt);
+  CK(cudaGetLastError());
+  return SDNS_OK;
+}
+
+// classic RK4 (spectralDNS/maths/integrators.py:149-159) on the caller-layout
+// state of a 3/2-rule context: u2 = u1 = u0; four stages; u0 = u2
+int rk4_step32(sdns_ctx* c, double dt) {
+  static const double ca[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+  static const double cb[3] = {0.5, 0.5, 1.0};
+  const size_t fb = 3 * c->nfull1 * c->csz;
+  CK(cudaMemcpyAsync(c->U32a, c->U32, fb, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemcpyAsync(c->U32b, c->U32, fb, cudaMemcpyDeviceToDevice, c->st));
+  int e;
+  for (int rk = 0; rk < 4; ++rk) {
+    if ((e = rhs32(c, c->U32, c->R32, rk == 3 && c->P32))) return e;
+    void* t[1] = {c->R32};
+    if (rk < 3) {
+      const double cf = cb[rk] * dt;
+      if ((e = lincomb_full(c, c->U32, c->U32a, 1, &cf, t))) return e;
+    }
+    const double cf2 = ca[rk] * dt;
+    if ((e = lincomb_full(c, c->U32b, c->U32b, 1, &cf2, t))) return e;
+  }
+  CK(cudaMemcpyAsync(c->U32, c->U32b, fb, cudaMemcpyDeviceToDevice, c->st));
+  k_time_step<<<1, 1, 0, c->st>>>(c->sc);
   CK(cudaGetLastError());
   return SDNS_OK;
 }
@@ -844,8 +929,8 @@ int sdns_create(const sdns_config* cfg, sdns_ctx** out) {
   }
   if (cfg->precision != SDNS_SINGLE && cfg->precision != SDNS_DOUBLE)
     return fail(SDNS_EINVAL, "precision must be SDNS_SINGLE or SDNS_DOUBLE");
-  if (cfg->dealias != SDNS_DEALIAS_23 && cfg->dealias != SDNS_DEALIAS_NONE)
-    return fail(SDNS_EINVAL, "dealias must be SDNS_DEALIAS_23 or SDNS_DEALIAS_NONE");
+  if (cfg->dealias != SDNS_DEALIAS_23 && cfg->dealias != SDNS_DEALIAS_NONE && cfg->dealias != SDNS_DEALIAS_32)
+    return fail(SDNS_EINVAL, "dealias must be SDNS_DEALIAS_23, SDNS_DEALIAS_NONE or SDNS_DEALIAS_32");
   if (cfg->formulation != SDNS_NS && cfg->formulation != SDNS_VV)
     return fail(SDNS_EINVAL, "formulation must be SDNS_NS or SDNS_VV");
   int ndev = 0;
@@ -860,6 +945,7 @@ int sdns_create(const sdns_config* cfg, sdns_ctx** out) {
   c->dev = cfg->device;
   c->dbl = cfg->precision == SDNS_DOUBLE;
   c->vv = cfg->formulation == SDNS_VV;
+  c->pad32 = cfg->dealias == SDNS_DEALIAS_32;
   c->rsz = c->dbl ? 8 : 4;
   c->csz = 2 * c->rsz;
   c->N0 = cfg->n[0]; c->N1 = cfg->n[1]; c->N2 = cfg->n[2]; c->N2h = c->N2 / 2 + 1;
@@ -886,17 +972,50 @@ int sdns_create(const sdns_config* cfg, sdns_ctx** out) {
     if (oe != 0) return bail(fail(SDNS_ECUDA, "shared-memory opt-in failed: %s", cudaGetErrorString((cudaError_t)oe)));
   }
   const long long cb = (long long)c->csz;
-  if ((e = dalloc(c, &c->Y, 3 * c->ncomp1 * cb))) return bail(e);
-  if ((e = dalloc(c, &c->S, 3 * c->ncomp1 * 16))) return bail(e);
-  if ((e = dalloc(c, &c->A, 3 * c->ncomp1 * 16))) return bail(e);
-  if ((e = dalloc(c, &c->T1, 6LL * c->N0 * c->K1 * c->Kzp * cb))) return bail(e);
-  if ((e = dalloc(c, &c->T2, 6LL * c->N0 * c->N1 * c->Kzp * cb))) return bail(e);
-  if (cfg->store_pressure && !c->vv && (e = dalloc(c, &c->Pc, c->ncomp1 * cb))) return bail(e);
+  if (c->pad32) {
+    // 3/2 rule: caller-layout state and RK4 vectors, padded scratch of M = 3N/2 per axis
+    for (int i = 0; i < 3; ++i) c->M[i] = 3 * cfg->n[i] / 2;
+    const long long f3 = 3 * c->nfull1 * cb;
+    const long long nm = (long long)c->M[0] * c->M[1] * (c->M[2] / 2 + 1);
+    const long long np = (long long)c->M[0] * c->M[1] * c->M[2];
+    if ((e = dalloc(c, &c->U32, f3))) return bail(e);
+    if ((e = dalloc(c, &c->U32a, f3))) return bail(e);
+    if ((e = dalloc(c, &c->U32b, f3))) return bail(e);
+    if ((e = dalloc(c, &c->R32, f3))) return bail(e);
+    if ((e = dalloc(c, &c->spec32, 6 * nm * cb))) return bail(e);
+    if ((e = dalloc(c, &c->phys32, 6 * np * (long long)c->rsz))) return bail(e);
+    if (cfg->store_pressure && !c->vv && (e = dalloc(c, &c->P32, c->nfull1 * cb))) return bail(e);
+    const int oe = pad32_smem_optin(c->dev, c->dbl);
+    if (oe != 0) return bail(fail(SDNS_ECUDA, "shared-memory opt-in failed: %s", cudaGetErrorString((cudaError_t)oe)));
+    long long tot = 0;
+    for (int i = 0; i < 3; ++i) { c->twoff32[i] = tot; tot += c->M[i]; }
+    std::vector<double> h(2 * tot);
+    for (int i = 0; i < 3; ++i)
+      for (int q = 0; q < c->M[i]; ++q) {
+        const double ang = -2.0 * M_PI * (double)q / (double)c->M[i];
+        h[2 * (c->twoff32[i] + q)] = cos(ang);
+        h[2 * (c->twoff32[i] + q) + 1] = sin(ang);
+      }
+    if ((e = dalloc(c, &c->tw32, tot * cb))) return bail(e);
+    std::vector<float> hf(2 * tot);
+    for (long long q = 0; q < 2 * tot; ++q) hf[q] = (float)h[q];
+    if (cudaMemcpy(c->tw32, c->dbl ? (const void*)h.data() : (const void*)hf.data(), tot * cb, cudaMemcpyHostToDevice) !=
+        cudaSuccess)
+      return bail(fail(SDNS_ECUDA, "twiddle upload failed"));
+    if (cudaMemset(c->U32, 0, f3) != cudaSuccess) return bail(fail(SDNS_ECUDA, "memset failed"));
+  } else {
+    if ((e = dalloc(c, &c->Y, 3 * c->ncomp1 * cb))) return bail(e);
+    if ((e = dalloc(c, &c->S, 3 * c->ncomp1 * 16))) return bail(e);
+    if ((e = dalloc(c, &c->A, 3 * c->ncomp1 * 16))) return bail(e);
+    if ((e = dalloc(c, &c->T1, 6LL * c->N0 * c->K1 * c->Kzp * cb))) return bail(e);
+    if ((e = dalloc(c, &c->T2, 6LL * c->N0 * c->N1 * c->Kzp * cb))) return bail(e);
+    if (cfg->store_pressure && !c->vv && (e = dalloc(c, &c->Pc, c->ncomp1 * cb))) return bail(e);
+    // blocks of the pointwise RK update (one energy/enstrophy partial pair each)
+    c->nblk_rk = (c->K1 * c->Kzp + 255) / 256 * c->K0;
+    if ((e = dalloc(c, &c->partials, 2 * c->nblk_rk * 8))) return bail(e);
+  }
   if ((e = dalloc(c, &c->sc, SC_COUNT * 8))) return bail(e);
   if ((e = dalloc(c, &c->flag, 16))) return bail(e);
-  // blocks of the pointwise RK update (one energy/enstrophy partial pair each)
-  c->nblk_rk = (c->K1 * c->Kzp + 255) / 256 * c->K0;
-  if ((e = dalloc(c, &c->partials, 2 * c->nblk_rk * 8))) return bail(e);
   // twiddle tables: per axis, pass tables [r][k] of W_{Ns R}^{r k} (forward)
   {
     long long tot = 0;
@@ -937,8 +1056,8 @@ int sdns_create(const sdns_config* cfg, sdns_ctx** out) {
     }
   }
   if (cudaMemset(c->sc, 0, SC_COUNT * 8) != cudaSuccess) return bail(fail(SDNS_ECUDA, "memset failed"));
-  if (cudaMemset(c->S, 0, 3 * c->ncomp1 * 16) != cudaSuccess) return bail(fail(SDNS_ECUDA, "memset failed"));
-  if (cudaMemset(c->Y, 0, 3 * c->ncomp1 * cb) != cudaSuccess) return bail(fail(SDNS_ECUDA, "memset failed"));
+  if (c->S && cudaMemset(c->S, 0, 3 * c->ncomp1 * 16) != cudaSuccess) return bail(fail(SDNS_ECUDA, "memset failed"));
+  if (c->Y && cudaMemset(c->Y, 0, 3 * c->ncomp1 * cb) != cudaSuccess) return bail(fail(SDNS_ECUDA, "memset failed"));
   *out = c;
   return SDNS_OK;
 }
@@ -949,7 +1068,8 @@ int sdns_destroy(sdns_ctx* c) {
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   void* bufs[] = {c->Y, c->S, c->A, c->T1, c->T2, c->Pc, c->Yx, c->src, c->src_full, c->H,
-                  c->F1, c->F2, c->PH, c->stage, c->tw, c->sc, c->partials, c->flag, c->red};
+                  c->F1, c->F2, c->PH, c->stage, c->tw, c->sc, c->partials, c->flag, c->red,
+                  c->U32, c->U32a, c->U32b, c->R32, c->P32, c->spec32, c->phys32, c->tw32};
   for (void* p : bufs)
     if (p) cudaFree(p);
   for (auto& e : c->evpool)
@@ -982,6 +1102,12 @@ int sdns_set_state(sdns_ctx* c, const void* u_hat, int where) {
   int e = check_ctx(c);
   if (e) return e;
   if (!u_hat) return fail(SDNS_EINVAL, "null u_hat");
+  if (c->pad32) {
+    if ((e = copy_in(c, c->U32, u_hat, 3 * c->nfull1 * (long long)c->csz, where))) return e;
+    CK(cudaStreamSynchronize(c->st));
+    c->has_state = true;
+    return SDNS_OK;
+  }
   if ((e = ensure_stage(c))) return e;
   if ((e = copy_in(c, c->stage, u_hat, 3 * c->nfull1 * (long long)c->csz, where))) return e;
   Geo g = geo(c);
@@ -1012,6 +1138,7 @@ int sdns_get_state(sdns_ctx* c, void* u_hat, int where) {
   int e = check_ctx(c);
   if (e) return e;
   if (!u_hat) return fail(SDNS_EINVAL, "null u_hat");
+  if (c->pad32) return copy_out(c, u_hat, c->U32, 3 * c->nfull1 * (long long)c->csz, where);
   if ((e = ensure_stage(c))) return e;
   Geo g = geo(c);
   if (c->dbl)
@@ -1034,6 +1161,12 @@ int sdns_set_source(sdns_ctx* c, const void* source, int where) {
     if (c->src_full) { cudaFree(c->src_full); c->bytes -= 3 * c->nfull1 * c->csz; c->src_full = nullptr; }
     return SDNS_OK;
   }
+  if (c->pad32) {  // the padded right-hand side reads the caller-layout source
+    if (!c->src_full && (e = dalloc(c, &c->src_full, 3 * c->nfull1 * (long long)c->csz))) return e;
+    if ((e = copy_in(c, c->src_full, source, 3 * c->nfull1 * (long long)c->csz, where))) return e;
+    CK(cudaStreamSynchronize(c->st));
+    return SDNS_OK;
+  }
   if (!c->src && (e = dalloc(c, &c->src, 3 * c->ncomp1 * 16))) return e;
   if (!c->src_full && (e = dalloc(c, &c->src_full, 3 * c->nfull1 * (long long)c->csz))) return e;
   if ((e = copy_in(c, c->src_full, source, 3 * c->nfull1 * (long long)c->csz, where))) return e;
@@ -1052,6 +1185,12 @@ int sdns_compute_rhs(sdns_ctx* c, const void* u_hat, void* rhs, int where) {
   if (e) return e;
   if (!u_hat || !rhs) return fail(SDNS_EINVAL, "null argument");
   if ((e = ensure_stage(c))) return e;
+  if (c->pad32) {
+    const long long fb3 = 3 * c->nfull1 * (long long)c->csz;
+    if ((e = copy_in(c, c->stage, u_hat, fb3, where))) return e;
+    if ((e = rhs32(c, c->stage, c->R32, c->P32 != nullptr))) return e;
+    return copy_out(c, rhs, c->R32, fb3, where);
+  }
   if (!c->Yx && (e = dalloc(c, &c->Yx, 3 * c->ncomp1 * (long long)c->csz))) return e;
   const long long fb = 3 * c->nfull1 * (long long)c->csz;
   if ((e = copy_in(c, c->stage, u_hat, fb, where))) return e;
@@ -1086,6 +1225,7 @@ int sdns_set_forcing(sdns_ctx* c, double eps, double kf) {
   int e = check_ctx(c);
   if (e) return e;
   if (c->vv && eps > 0) return fail(SDNS_EINVAL, "the forcing is defined for the velocity formulation (SDNS_NS) only");
+  if (c->pad32 && eps > 0) return fail(SDNS_EINVAL, "the forcing is not available with the 3/2 rule");
   c->eps = eps > 0 ? eps : 0;
   c->kf = kf;
   c->gkey = ~0ull;
@@ -1095,6 +1235,7 @@ int sdns_set_forcing(sdns_ctx* c, double eps, double kf) {
 int sdns_set_cfl(sdns_ctx* c, double cfl) {
   int e = check_ctx(c);
   if (e) return e;
+  if (c->pad32 && cfl > 0) return fail(SDNS_EINVAL, "the CFL time step is not available with the 3/2 rule");
   c->cfl = cfl > 0 ? cfl : 0;
   c->gkey = ~0ull;
   c->last_dt = -1;
@@ -1121,6 +1262,11 @@ int sdns_rk4(sdns_ctx* c, double dt, int32_t nsteps) {
       CK(cudaStreamSynchronize(c->st));
       c->last_dt = dt;
     }
+  }
+  if (c->pad32) {
+    for (int s = 0; s < nsteps; ++s)
+      if ((e = rk4_step32(c, dt))) return e;
+    return SDNS_OK;
   }
   if (c->timing) {
     for (int k = 0; k < 8; ++k) { c->tms[k] = 0; c->tcount[k] = 0; }
@@ -1250,6 +1396,13 @@ int sdns_pressure(sdns_ctx* c, void* p, int where) {
   int e = check_ctx(c);
   if (e) return e;
   if (c->vv) return fail(SDNS_EINVAL, "the velocity-vorticity formulation has no pressure (VV.py:27)");
+  if (c->pad32) {
+    if (!c->P32) return fail(SDNS_ESTATE, "pressure is not stored (create the context with store_pressure=1)");
+    if ((e = ensure_full_bufs(c))) return e;
+    if ((e = repitch(c, c->P32, c->F1, 1, c->N2h, c->Kzpf, c->N2h))) return e;
+    if ((e = full_backward(c, c->F1, c->F2, 1))) return e;
+    return copy_out(c, p, c->PH, c->nphys1 * (long long)c->rsz, where);
+  }
   if (!c->Pc) return fail(SDNS_ESTATE, "pressure is not stored (create the context with store_pressure=1)");
   if ((e = ensure_full_bufs(c))) return e;
   Geo g = geo(c);
@@ -1269,14 +1422,14 @@ int sdns_diagnostics(sdns_ctx* c, double* out) {
   if (e) return e;
   if (!out) return fail(SDNS_EINVAL, "null out");
   if (!c->has_state) return fail(SDNS_ESTATE, "no state set");
-  Geo g = geo(c);
+  Geo g = diag_geo(c);
   const unsigned nb = 152 * 4;
   double* part = nullptr;
   if ((e = dalloc(c, &part, 3LL * nb * 8))) return e;
   if (c->dbl)
-    k_diag<double2><<<nb, 256, 0, c->st>>>(c->S, c->high ? (const double2*)c->H : nullptr, g, c->ncomp1, part, c->vv);
+    k_diag<double2><<<nb, 256, 0, c->st>>>(c->S, (const double2*)diag_full(c), g, c->ncomp1, part, c->vv);
   else
-    k_diag<float2><<<nb, 256, 0, c->st>>>(c->S, c->high ? (const float2*)c->H : nullptr, g, c->ncomp1, part, c->vv);
+    k_diag<float2><<<nb, 256, 0, c->st>>>(c->S, (const float2*)diag_full(c), g, c->ncomp1, part, c->vv);
   CK(cudaGetLastError());
   std::vector<double> h(3 * nb);
   double scal[SC_COUNT];
@@ -1308,13 +1461,13 @@ int sdns_spectrum(sdns_ctx* c, double* Ek, int32_t nbins) {
   double* d = nullptr;
   if ((e = dalloc(c, &d, 2LL * nbins * 8))) return e;
   CK(cudaMemsetAsync(d, 0, 2LL * nbins * 8, c->st));
-  Geo g = geo(c);
+  Geo g = diag_geo(c);
   if (c->dbl)
-    k_spectrum<double2><<<152 * 4, 256, 0, c->st>>>(c->S, c->high ? (const double2*)c->H : nullptr, g, c->ncomp1, d,
-                                                   d + nbins, nbins, c->vv);
+    k_spectrum<double2><<<152 * 4, 256, 0, c->st>>>(c->S, (const double2*)diag_full(c), g, c->ncomp1, d, d + nbins,
+                                                   nbins, c->vv);
   else
-    k_spectrum<float2><<<152 * 4, 256, 0, c->st>>>(c->S, c->high ? (const float2*)c->H : nullptr, g, c->ncomp1, d,
-                                                  d + nbins, nbins, c->vv);
+    k_spectrum<float2><<<152 * 4, 256, 0, c->st>>>(c->S, (const float2*)diag_full(c), g, c->ncomp1, d, d + nbins,
+                                                  nbins, c->vv);
   CK(cudaGetLastError());
   std::vector<double> h(2 * nbins);
   CK(cudaMemcpyAsync(h.data(), d, 2LL * nbins * 8, cudaMemcpyDeviceToHost, c->st));

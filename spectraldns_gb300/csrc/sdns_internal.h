@@ -107,6 +107,26 @@ struct RKArgs {
                              // convective term is i K x (nonlinear term), no projection
 };
 
+// 3/2-rule (padded) right-hand side: grid N, padded grid M = 3N/2 per axis
+struct Pad32 {
+  int N[3], M[3];
+  double ks[3];              // 2 pi / L
+  double nu;
+  bool dbl, vv;
+  void* spec;                // [6][M0][M1][M2/2+1] complex scratch
+  void* phys;                // [6][M0][M1][M2] real scratch
+  const void* tw[3];         // W_{M_i}^j = exp(-2 pi i j / M_i), j < M_i, per axis
+};
+// one strided axis of the padded transforms (see k_fft_axis)
+struct Pad32Axis {
+  int n, W;
+  long long nlines, B, fs, ss, rs;
+};
+// rhs (caller layout) of u_hat (caller layout), + src if not null; phat
+// (NS only, may be null) receives the pressure coefficient P_hat
+int pad32_rhs(const Pad32& p, const void* u_hat, const void* src, void* rhs, void* phat, cudaStream_t s);
+int pad32_smem_optin(int dev, bool dbl);
+
 // message returned by sdns_last_error() (thread-local)
 void set_last_error(const char* msg);
 

@@ -36,8 +36,9 @@ class Context:
         self.nu = float(nu)
         if precision not in ("single", "double"):
             raise ValueError("precision must be 'single' or 'double'")
-        if dealias not in ("2/3-rule", "None"):
-            raise ValueError("dealias %r is not supported by the GPU backend (2/3-rule or None)" % (dealias,))
+        if dealias not in ("2/3-rule", "3/2-rule", "None"):
+            raise ValueError("dealias %r is not supported by the GPU backend (2/3-rule, 3/2-rule or None)"
+                             % (dealias,))
         if formulation not in ("NS", "VV"):
             raise ValueError("formulation must be 'NS' (velocity) or 'VV' (velocity-vorticity)")
         self.precision = precision
@@ -54,7 +55,8 @@ class Context:
         cfg.L[:] = self.L
         cfg.nu = self.nu
         cfg.precision = _lib.SDNS_SINGLE if precision == "single" else _lib.SDNS_DOUBLE
-        cfg.dealias = _lib.SDNS_DEALIAS_23 if dealias == "2/3-rule" else _lib.SDNS_DEALIAS_NONE
+        cfg.dealias = {"2/3-rule": _lib.SDNS_DEALIAS_23, "3/2-rule": _lib.SDNS_DEALIAS_32,
+                       "None": _lib.SDNS_DEALIAS_NONE}[dealias]
         cfg.device = self.device
         cfg.store_pressure = 1 if store_pressure and formulation == "NS" else 0
         cfg.formulation = _lib.SDNS_VV if formulation == "VV" else _lib.SDNS_NS

@@ -182,16 +182,13 @@ def get_context(formulation="NS"):
     velocity-vorticity solver, spectraldns_gb300.solvers.VV, builds on this).
     """
     float_, complex_, mpitype = datatypes(params.precision)
-    if params.dealias == "3/2-rule":
-        raise ValueError("the GB300 backend implements the 2/3 rule (and 'None'); the 3/2 rule is not supported")
     if params.dealias == "None" and not params.mask_nyquist:
         raise ValueError("the GB300 backend masks the Nyquist modes when dealias is 'None'")
     if params.convection != "Vortex":
         raise ValueError("the GB300 backend implements the Vortex convection form")
     N = tuple(int(n) for n in params.N)
     L = tuple(float(x) for x in params.L)
-    gpu = Context(N, L, nu=float(params.nu), precision=params.precision,
-                  dealias="2/3-rule" if params.dealias == "2/3-rule" else "None",
+    gpu = Context(N, L, nu=float(params.nu), precision=params.precision, dealias=params.dealias,
                   device=int(params.get("device", 0)), store_pressure=formulation == "NS",
                   formulation=formulation)
     T = Space(gpu, 1)

@@ -138,3 +138,39 @@ def test_vv_known_answers(N, L):
     assert round(0.5 * g.mean_square(U) - 0.124953117517, 7) == 0
     assert round(0.5 * g.mean_square(g.backward(wh)) - 0.375249930801, 7) == 0
     assert np.max(np.abs(wh - g.curl_hat(uh))) < 1e-13
+
+
+@pytest.mark.parametrize("N,L", [((16, 16, 16), (2 * np.pi,) * 3), ((64, 32, 16), (6 * np.pi, 4 * np.pi, 2 * np.pi))])
+def test_three_halves_rule_known_answers(N, L):
+    """tests/test_NSVV.py::test_solvers reruns TG with dealias '3/2-rule' against tests/TG.py:125-126."""
+    g = Grid(N, L, dealias="3/2-rule")
+    uh = g.forward(taylor_green(g))
+    for _ in range(10):
+        uh = g.rk4_step(uh, 0.01)
+    assert round(g.kinetic_energy(uh) - 0.124953117517, 7) == 0
+    assert round(g.enstrophy(uh) - 0.375249930801, 7) == 0
+
+
+def test_three_halves_rule_is_alias_free():
+    """The padded product of two N-mode fields equals the exact product (formed on a 2N grid,
+    where a quadratic term cannot alias), truncated to the N modes."""
+    g = Grid((16, 16, 16), dealias="3/2-rule")
+    rng = np.random.default_rng(0)
+    a = g.forward(rng.standard_normal((3, 16, 16, 16))) * g.mask
+    b = g.forward(rng.standard_normal((3, 16, 16, 16))) * g.mask
+    nl = g._nonlinear(a, b)
+    g2 = Grid((32, 32, 32))
+    i0, t0, kz = np.r_[0:8, 9:16], np.r_[0:8, 25:32], np.arange(8)
+    src = (slice(None), i0[:, None, None], i0[None, :, None], kz[None, None, :])
+    dst = (slice(None), t0[:, None, None], t0[None, :, None], kz[None, None, :])
+
+    def up(x):
+        X = np.zeros((3, 32, 32, 17), complex)
+        X[dst] = x[src]
+        return X
+    ex = g2.forward(g2.cross(g2.backward(up(a)), g2.backward(up(b))))
+    exs = np.zeros_like(nl)
+    exs[src] = ex[dst]
+    assert np.abs(nl - exs).max() < 1e-14 * np.abs(exs).max()
+    # the 2/3 rule on the same (unpadded) grid is a different, truncating approximation
+    assert np.abs(Grid((16, 16, 16))._nonlinear(a, b) - exs).max() > 1e-3 * np.abs(exs).max()
