@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-les", action="store_true", help="skip the closure-LES timing")
     p.add_argument("--no-1024", action="store_true", help="skip the 1024^3 decaying-turbulence timing")
+    p.add_argument("--no-pad32", action="store_true", help="skip the 3/2-rule timing")
+    p.add_argument("--no-cufft", action="store_true", help="skip the same-GPU cuFFT (torch.fft) comparison")
     p.add_argument("--grid", default=None,
                    help="N0,N1,N2: run the workload on this (small, profiling) grid instead of --n cubed")
     p.add_argument("--tg256", action="store_true",
@@ -298,6 +300,10 @@ def run_ours(args):
         out["les"] = les_measure(dev, n, dns_s_per_sim_time)
     if not args.no_1024 and n == 512:
         out["decaying_1024"] = decay_1024(dev, ws)
+    if not args.no_pad32 and n == 512:
+        out["dealias_3_2"] = pad32_line(dev, ws)
+    if not args.no_cufft:
+        out["cufft_comparison"] = cufft_compare(dev, ws, N, out["value"])
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_sample(512 if n >= 512 else n)
     if rank == 0:
@@ -374,6 +380,106 @@ def decay_1024(dev, ws, steps=5):
            "workload": "decaying isotropic turbulence 1024^3 FP32 (seeded k^4 exp(-2(k/6)^2), E=0.5, "
                        "nu=4e-4, no forcing, RK4 CFL 0.5, FP64 reductions)"}
     c.close()
+    return res
+
+
+def cufft_compare(dev, ws, N, ours_steps_per_s, steps=5, dt=1e-3):
+    """The same RK4 step written with cuFFT (torch.fft.rfftn / irfftn) and torch pointwise kernels on
+    this GPU: the 2/3-rule Vortex right-hand side of spectralDNS NS.py:219-261 on full spectral arrays,
+    FP32, fixed dt, no forcing.  A comparison arm only: it is not part of the library.  Reports its
+    steps/s, our steps/s over it, and the relative difference of one right-hand side computed both ways."""
+    import torch
+    from spectraldns_gb300.gpu import Context
+    from spectraldns_gb300.init import isotropic_field
+    d = torch.device("cuda", dev)
+    n0, n1, n2 = N
+    kc = [int(math.ceil(2.0 / 3.0 * (n // 2 + 1))) - 1 for n in N]
+    for i, n in enumerate(N):  # largest |k| < 2/3 (n/2 + 1)
+        while kc[i] >= 2.0 / 3.0 * (n // 2 + 1):
+            kc[i] -= 1
+    k0 = torch.fft.fftfreq(n0, 1.0 / n0, device=d).float().view(-1, 1, 1)
+    k1 = torch.fft.fftfreq(n1, 1.0 / n1, device=d).float().view(1, -1, 1)
+    k2 = torch.arange(n2 // 2 + 1, device=d).float().view(1, 1, -1)
+    mask = ((k0.abs() <= kc[0]) & (k1.abs() <= kc[1]) & (k2 <= kc[2])).to(torch.complex64)
+    K = [k0, k1, k2]
+    K2 = k0 * k0 + k1 * k1 + k2 * k2
+    iK2 = torch.where(K2 == 0, torch.zeros_like(K2), 1.0 / torch.where(K2 == 0, torch.ones_like(K2), K2))
+    scale = float(n0 * n1 * n2)
+
+    def rhs(uh):
+        um = uh * mask
+        u = torch.fft.irfftn(um, s=N, dim=(1, 2, 3)) * scale
+        w = torch.fft.irfftn(torch.stack([1j * (K[1] * um[2] - K[2] * um[1]), 1j * (K[2] * um[0] - K[0] * um[2]),
+                                          1j * (K[0] * um[1] - K[1] * um[0])]), s=N, dim=(1, 2, 3)) * scale
+        x = torch.stack([u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]])
+        nl = torch.fft.rfftn(x, dim=(1, 2, 3)) / scale * mask
+        P = (nl[0] * K[0] + nl[1] * K[1] + nl[2] * K[2]) * iK2
+        return torch.stack([nl[c] - P * K[c] - NU * K2 * uh[c] for c in range(3)])
+
+    a, b = (1 / 6, 1 / 3, 1 / 3, 1 / 6), (0.5, 0.5, 1.0)
+
+    def step(u0):
+        u1 = u0
+        u2 = u0.clone()
+        for rk in range(4):
+            r = rhs(u0)
+            if rk < 3:
+                u0 = u1 + (b[rk] * dt) * r
+            u2 += (a[rk] * dt) * r
+        return u2
+
+    uh0 = isotropic_field(N, k0=K0, energy=0.5, seed=0, dtype=np.complex64)
+    uh = torch.from_numpy(uh0).to(d)
+    ref = rhs(uh)
+    c = Context(N, nu=NU, precision="single", device=dev)
+    ours = c.compute_rhs(uh.contiguous())
+    diff = float((ours - ref).abs().max() / ref.abs().max())
+    c.close()
+    del ours, ref
+    for _ in range(2):
+        uh = step(uh)
+    torch.cuda.synchronize(d)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        uh = step(uh)
+    e1.record()
+    torch.cuda.synchronize(d)
+    ms = e0.elapsed_time(e1) / steps
+    v = ws * 1e3 / ms
+    return {"value": v, "unit": "steps/s", "ms_per_step": ms, "steps": steps, "warmup": 2, "dtype": "f32",
+            "ours_over_cufft": ours_steps_per_s / v if v > 0 else None, "rhs_max_rel_diff_vs_ours": diff,
+            "what": "torch.fft (cuFFT) rfftn/irfftn + torch pointwise kernels, full spectral arrays, 2/3 mask, "
+                    "projection, diffusion, classic RK4 in FP32, fixed dt %g" % dt}
+
+
+def pad32_line(dev, ws, n=256, steps=10):
+    """RK4 steps/s of the same seeded isotropic field at n^3 FP32 (fixed dt) with the 3/2 rule (padded
+    3n/2 transforms, generic mixed-radix kernels) and with the 2/3 rule (fused sweeps), for the cost of
+    the reference's second dealiasing mode."""
+    import torch
+    from spectraldns_gb300.gpu import Context
+    from spectraldns_gb300.init import isotropic_field
+    N = (n,) * 3
+    uh = isotropic_field(N, k0=K0, energy=0.5, seed=0, dtype=np.complex64)
+    res = {"grid": list(N), "dtype": "f32", "steps": steps, "warmup": 3, "dt": 1e-3, "unit": "steps/s"}
+    for rule, key in (("3/2-rule", "three_halves"), ("2/3-rule", "two_thirds")):
+        c = Context(N, nu=NU, precision="single", dealias=rule, device=dev)
+        c.set_state(uh)
+        c.rk4(1e-3, 3)
+        c.synchronize()
+        st = torch.cuda.ExternalStream(c.stream_handle(), device=torch.device("cuda", dev))
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(st)
+        c.rk4(1e-3, steps)
+        a1.record(st)
+        torch.cuda.synchronize(dev)
+        ms = a0.elapsed_time(a1)
+        res[key] = ws * steps / (ms / 1e3)
+        res[key + "_hbm_bytes"] = c.memory_bytes()
+        c.close()
     return res
 
 

@@ -121,6 +121,10 @@ struct Pad32 {
 struct Pad32Axis {
   int n, W;
   long long nlines, B, fs, ss, rs;
+  // lines that can be nonzero: l = a * ld2 + kz with kz < kzmax and (na > 0) a
+  // in the N-grid band of an axis of ma points; ld2 = 0: every line
+  long long ld2;
+  int kzmax, na, ma;
 };
 // rhs (caller layout) of u_hat (caller layout), + src if not null; phat
 // (NS only, may be null) receives the pressure coefficient P_hat

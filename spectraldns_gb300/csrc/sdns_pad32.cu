@@ -12,6 +12,8 @@
 // 2/3-rule sweeps remain the fast path.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "sdns_fft.cuh"
 #include "sdns_internal.h"
 
@@ -47,68 +49,98 @@ __device__ __forceinline__ void dft_small(C* v, int r, int s) {
   }
 }
 
-// Stockham autosort FFT (Govindaraju et al., SC'08) of W lines of length n
-// (pitch ld) held in shared memory, ping-ponging between a and b; returns the
-// buffer holding the result.  tw[j] = exp(-2 pi i j / n) (FP64, rounded);
-// s = -1 forward, +1 inverse (unnormalised).
-template <typename C>
-__device__ C* smem_fft(C* a, C* b, int W, int n, int ld, int s, const C* __restrict__ tw) {
-  C* in = a;
-  C* out = b;
-  int ns = 1;
-  while (ns < n) {
-    const int rem = n / ns;
-    const int r = (rem % 4 == 0) ? 4 : (rem % 2 == 0 ? 2 : 3);
-    const int nb = n / r, tstride = n / (ns * r);
-    for (int t = threadIdx.x; t < W * nb; t += blockDim.x) {
-      const int w = t / nb, j = t - w * nb;
-      const int k = j % ns;
-      const C* x = in + w * ld;
-      C* y = out + w * ld;
+// Stockham autosort FFT (Govindaraju et al., SC'08) of W lines of length N
+// (pitch N + 1) held in shared memory, ping-ponging between a and b; returns
+// the buffer holding the result.  The radix sequence (4s, then a 2, then a 3)
+// and every stride are compile-time constants.  tw[j] = exp(-2 pi i j / N)
+// (FP64, rounded); s = -1 forward, +1 inverse (unnormalised).
+template <int N, int NS> struct pass_radix {
+  static constexpr int rem = N / NS;
+  static constexpr int value = rem % 4 == 0 ? 4 : (rem % 2 == 0 ? 2 : 3);
+};
+
+template <typename C, int N, int NS>
+__device__ __forceinline__ C* fft_passes(C* in, C* out, int W, int s, const C* __restrict__ tw) {
+  if constexpr (NS >= N) {
+    return in;
+  } else {
+    constexpr int R = pass_radix<N, NS>::value, NB = N / R, TS = N / (NS * R), LD = N + 1;
+    for (int t = threadIdx.x; t < W * NB; t += blockDim.x) {
+      const int w = t / NB, j = t - w * NB;
+      const int k = j % NS;
+      const C* x = in + w * LD;
+      C* y = out + w * LD;
       C v[4];
-      for (int m = 0; m < r; ++m) v[m] = x[j + m * nb];
-      for (int m = 1; m < r; ++m) {
-        C wv = tw[(tstride * k * m) % n];
+#pragma unroll
+      for (int m = 0; m < R; ++m) v[m] = x[j + m * NB];
+#pragma unroll
+      for (int m = 1; m < R; ++m) {
+        C wv = tw[TS * k * m];
         if (s > 0) wv.y = -wv.y;
         v[m] = cmul(v[m], wv);
       }
-      dft_small(v, r, s);
-      const int base = (j / ns) * ns * r + k;
-      for (int m = 0; m < r; ++m) y[base + m * ns] = v[m];
+      dft_small(v, R, s);
+      const int base = (j / NS) * NS * R + k;
+#pragma unroll
+      for (int m = 0; m < R; ++m) y[base + m * NS] = v[m];
     }
     __syncthreads();
-    C* tmp = in;
-    in = out;
-    out = tmp;
-    ns *= r;
+    return fft_passes<C, N, NS * R>(out, in, W, s, tw);
   }
-  return in;
+}
+
+template <typename C, int N>
+__device__ __forceinline__ C* smem_fft(C* a, C* b, int W, int s, const C* __restrict__ tw) {
+  return fft_passes<C, N, 1>(a, b, W, s, tw);
+}
+
+// Is line l of a padded axis sweep one that can hold nonzero data?  Lines are
+// (a, kz) with a = l / ld2 and kz = l % ld2: kz must be below kzmax and, when
+// na > 0, a must be one of the N-grid wave numbers of an axis of length ma
+// (a < na/2 or a > ma - na/2).  Lines that cannot are all zero on input (the
+// inverse sweeps) or never read (the forward sweeps) and are skipped.
+__device__ __forceinline__ bool line_live(long long l, const Pad32Axis& ax) {
+  if (ax.ld2 <= 0) return true;
+  const long long a = l / ax.ld2;
+  const int kz = (int)(l - a * ax.ld2);
+  if (kz >= ax.kzmax) return false;
+  return ax.na <= 0 || 2 * a < ax.na || 2 * (ax.ma - a) < ax.na;
 }
 
 // C2C along a strided axis, in place: line l of field f starts at
 // f*fs + (l / B)*ss + (l % B), position p adds p*rs.  A block transforms W
-// adjacent lines (coalesced rows of W values).
-template <typename C>
+// adjacent lines (coalesced rows of W values); tiles without a live line return.
+template <typename C, int N>
 __global__ void __launch_bounds__(256) k_fft_axis(C* data, Pad32Axis ax, int s, double scale, const C* tw) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int n = ax.n, W = ax.W, ld = n + 1;
+  constexpr int n = N, ld = N + 1;
+  const int W = ax.W;
   C* a = reinterpret_cast<C*>(smraw);
   C* b = a + (size_t)W * ld;
   const long long l0 = (long long)blockIdx.x * W;
   const long long nl = ax.nlines;
+  {
+    bool any = false;
+    for (int w = 0; w < W; ++w)
+      if (l0 + w < nl && line_live(l0 + w, ax)) { any = true; break; }
+    if (!any) return;
+  }
+  // every row of the tile is in flight at once (cp.async), then one wait
   for (int idx = threadIdx.x; idx < W * n; idx += blockDim.x) {
     const int w = idx % W, p = idx / W;
     const long long l = l0 + w;
     if (l < nl) {
       const long long f = blockIdx.y;
       const long long o = f * ax.fs + (l / ax.B) * ax.ss + (l % ax.B) + (long long)p * ax.rs;
-      a[w * ld + p] = data[o];
+      cp_async<sizeof(C)>(&a[w * ld + p], &data[o]);
     } else {
       a[w * ld + p] = cz<C>();
     }
   }
+  cp_commit();
+  cp_wait_all();
   __syncthreads();
-  const C* res = smem_fft(a, b, W, n, ld, s, tw);
+  const C* res = smem_fft<C, N>(a, b, W, s, tw);
   using Real = decltype(C::x);
   const Real sc = (Real)scale;
   for (int idx = threadIdx.x; idx < W * n; idx += blockDim.x) {
@@ -126,35 +158,60 @@ __global__ void __launch_bounds__(256) k_fft_axis(C* data, Pad32Axis ax, int s, 
 // C2R (dir > 0) or R2C (dir < 0) along the contiguous last axis.  Spectral
 // lines have nh = n/2 + 1 values (pitch nh), physical lines n values.  C2R
 // drops the imaginary parts of the k = 0 and k = n/2 coefficients.
-template <typename C>
-__global__ void __launch_bounds__(256) k_fft_z(C* spec, void* physv, long long nlines, int n, int W, int dir,
-                                               double scale, const C* tw) {
+template <typename C, int N>
+__global__ void __launch_bounds__(256) k_fft_z(C* spec, void* physv, long long nlines, int W, int dir, double scale,
+                                               const C* tw) {
   using Real = decltype(C::x);
   Real* phys = reinterpret_cast<Real*>(physv);
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int nh = n / 2 + 1, ld = n + 1;
+  constexpr int n = N, nh = N / 2 + 1, ld = N + 1;
   C* a = reinterpret_cast<C*>(smraw);
   C* b = a + (size_t)W * ld;
   const long long l0 = (long long)blockIdx.x * W;
   if (dir > 0) {
+    // stage the half spectra (cp.async, all in flight), then form the Hermitian lines
     for (int idx = threadIdx.x; idx < W * nh; idx += blockDim.x) {
       const int w = idx / nh, k = idx - w * nh;
       const long long l = l0 + w;
-      C v = cz<C>();
-      if (l < nlines) v = spec[l * nh + k];
-      if (k == 0 || 2 * k == n) v.y = 0;
-      a[w * ld + k] = v;
-      if (k > 0 && 2 * k < n) a[w * ld + n - k] = mk<C>(v.x, -v.y);
+      if (l < nlines) cp_async<sizeof(C)>(&a[w * ld + k], &spec[l * nh + k]);
+      else a[w * ld + k] = cz<C>();
+    }
+    cp_commit();
+    cp_wait_all();
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < W * nh; idx += blockDim.x) {
+      const int w = idx / nh, k = idx - w * nh;
+      C v = a[w * ld + k];
+      if (k == 0 || 2 * k == n) {
+        v.y = 0;
+        a[w * ld + k] = v;
+      } else {
+        a[w * ld + n - k] = mk<C>(v.x, -v.y);
+      }
     }
   } else {
-    for (int idx = threadIdx.x; idx < W * n; idx += blockDim.x) {
-      const int w = idx / n, j = idx - w * n;
-      const long long l = l0 + w;
-      a[w * ld + j] = mk<C>(l < nlines ? phys[l * n + j] : (Real)0, (Real)0);
+    // real lines: eight independent loads per thread before the shared-memory stores
+    constexpr int U = 8;
+    for (int base = threadIdx.x; base < W * n; base += U * blockDim.x) {
+      Real r[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int idx = base + u * blockDim.x;
+        const int w = idx / n;
+        r[u] = (idx < W * n && l0 + w < nlines) ? phys[(l0 + w) * n + (idx - w * n)] : (Real)0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int idx = base + u * blockDim.x;
+        if (idx < W * n) {
+          const int w = idx / n;
+          a[w * ld + idx - w * n] = mk<C>(r[u], (Real)0);
+        }
+      }
     }
   }
   __syncthreads();
-  const C* res = smem_fft(a, b, W, n, ld, dir > 0 ? 1 : -1, tw);
+  const C* res = smem_fft<C, N>(a, b, W, dir > 0 ? 1 : -1, tw);
   const Real sc = (Real)scale;
   if (dir > 0) {
     for (int idx = threadIdx.x; idx < W * n; idx += blockDim.x) {
@@ -295,6 +352,20 @@ inline int tile_lines(int n, size_t csz) {
   return W;
 }
 
+// launch a kernel instance templated on the padded length M in {24, ..., 1536}
+template <typename F> int by_length(int n, F&& f) {
+  switch (n) {
+    case 24: return f(std::integral_constant<int, 24>());
+    case 48: return f(std::integral_constant<int, 48>());
+    case 96: return f(std::integral_constant<int, 96>());
+    case 192: return f(std::integral_constant<int, 192>());
+    case 384: return f(std::integral_constant<int, 384>());
+    case 768: return f(std::integral_constant<int, 768>());
+    case 1536: return f(std::integral_constant<int, 1536>());
+    default: return (int)cudaErrorInvalidValue;
+  }
+}
+
 template <typename C> int rhs_t(const Pad32& p, const void* u_hat, const void* src, void* rhs, void* phat,
                                 cudaStream_t s) {
   using Real = decltype(C::x);
@@ -306,34 +377,42 @@ template <typename C> int rhs_t(const Pad32& p, const void* u_hat, const void* s
   const C* tw1 = reinterpret_cast<const C*>(p.tw[1]);
   const C* tw2 = reinterpret_cast<const C*>(p.tw[2]);
   k_pad_fields<C><<<grid_for(nm), 256, 0, s>>>(reinterpret_cast<const C*>(u_hat), spec, p);
+  int err = 0;
+  // lines (a, kz) of the x sweeps: a = k1 position; of the y sweeps: a = k0 position (any)
   auto axis = [&](int n, long long nlines, long long B, long long fs, long long ss, long long rs, int nf, int sign,
-                  double scale, const C* tw) {
+                  double scale, const C* tw, int na, int ma) {
     Pad32Axis ax;
     ax.n = n; ax.nlines = nlines; ax.B = B; ax.fs = fs; ax.ss = ss; ax.rs = rs;
+    ax.ld2 = M2h; ax.kzmax = p.N[2] / 2; ax.na = na; ax.ma = ma;
     ax.W = tile_lines(n, sizeof(C));
     const size_t sm = (size_t)2 * ax.W * (n + 1) * sizeof(C);
     const dim3 grid((unsigned)((nlines + ax.W - 1) / ax.W), (unsigned)nf);
-    k_fft_axis<C><<<grid, 256, sm, s>>>(spec, ax, sign, scale, tw);
+    const int e = by_length(n, [&](auto L) {
+      k_fft_axis<C, decltype(L)::value><<<grid, 256, sm, s>>>(spec, ax, sign, scale, tw);
+      return (int)cudaGetLastError();
+    });
+    if (e && !err) err = e;
+  };
+  auto zpass = [&](int nf, int dir) {
+    const int W = tile_lines(M2, sizeof(C));
+    const size_t sm = (size_t)2 * W * (M2 + 1) * sizeof(C);
+    const long long nl = (long long)nf * M0 * M1;
+    const int e = by_length(M2, [&](auto L) {
+      k_fft_z<C, decltype(L)::value><<<(unsigned)((nl + W - 1) / W), 256, sm, s>>>(spec, ph, nl, W, dir, 1.0, tw2);
+      return (int)cudaGetLastError();
+    });
+    if (e && !err) err = e;
   };
   // inverse: x (lines M1*M2h, rows stride M1*M2h), y (lines M0*M2h in runs of M2h), z C2R
-  axis(M0, (long long)M1 * M2h, (long long)M1 * M2h, nm, 0, (long long)M1 * M2h, 6, +1, 1.0, tw0);
-  axis(M1, (long long)M0 * M2h, M2h, nm, (long long)M1 * M2h, M2h, 6, +1, 1.0, tw1);
-  {
-    const int W = tile_lines(M2, sizeof(C));
-    const size_t sm = (size_t)2 * W * (M2 + 1) * sizeof(C);
-    const long long nl = 6LL * M0 * M1;
-    k_fft_z<C><<<(unsigned)((nl + W - 1) / W), 256, sm, s>>>(spec, ph, nl, M2, W, +1, 1.0, tw2);
-  }
+  axis(M0, (long long)M1 * M2h, (long long)M1 * M2h, nm, 0, (long long)M1 * M2h, 6, +1, 1.0, tw0, p.N[1], M1);
+  axis(M1, (long long)M0 * M2h, M2h, nm, (long long)M1 * M2h, M2h, 6, +1, 1.0, tw1, 0, M0);
+  zpass(6, +1);
   k_cross6<Real><<<grid_for(np), 256, 0, s>>>(ph, np);
-  {
-    const int W = tile_lines(M2, sizeof(C));
-    const size_t sm = (size_t)2 * W * (M2 + 1) * sizeof(C);
-    const long long nl = 3LL * M0 * M1;
-    k_fft_z<C><<<(unsigned)((nl + W - 1) / W), 256, sm, s>>>(spec, ph, nl, M2, W, -1, 1.0, tw2);
-  }
-  axis(M1, (long long)M0 * M2h, M2h, nm, (long long)M1 * M2h, M2h, 3, -1, 1.0, tw1);
+  zpass(3, -1);
+  axis(M1, (long long)M0 * M2h, M2h, nm, (long long)M1 * M2h, M2h, 3, -1, 1.0, tw1, 0, M0);
   axis(M0, (long long)M1 * M2h, (long long)M1 * M2h, nm, 0, (long long)M1 * M2h, 3, -1,
-       1.0 / ((double)M0 * M1 * M2), tw0);
+       1.0 / ((double)M0 * M1 * M2), tw0, p.N[1], M1);
+  if (err) return err;
   const long long f1 = (long long)p.N[0] * p.N[1] * (p.N[2] / 2 + 1);
   k_rhs32<C><<<grid_for(f1), 256, 0, s>>>(spec, reinterpret_cast<const C*>(u_hat), reinterpret_cast<const C*>(src),
                                           reinterpret_cast<C*>(rhs), reinterpret_cast<C*>(phat), p);
@@ -343,8 +422,14 @@ template <typename C> int rhs_t(const Pad32& p, const void* u_hat, const void* s
 template <typename C> cudaError_t optin(int dev) {
   int mx = 0;
   cudaError_t e = cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fft_axis<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fft_z<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  for (int n : {24, 48, 96, 192, 384, 768, 1536}) {
+    by_length(n, [&](auto L) {
+      constexpr int NL = decltype(L)::value;
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fft_axis<C, NL>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fft_z<C, NL>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+      return 0;
+    });
+  }
   return e;
 }
 
