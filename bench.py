@@ -54,6 +54,8 @@ def parse():
     p.add_argument("--no-1024", action="store_true", help="skip the 1024^3 decaying-turbulence timing")
     p.add_argument("--no-pad32", action="store_true", help="skip the 3/2-rule timing")
     p.add_argument("--no-cufft", action="store_true", help="skip the same-GPU cuFFT (torch.fft) comparison")
+    p.add_argument("--precision", default="single", choices=("single", "double"),
+                   help="precision of the main workload (profiling the FP64 kernels); the headline is single")
     p.add_argument("--grid", default=None,
                    help="N0,N1,N2: run the workload on this (small, profiling) grid instead of --n cubed")
     p.add_argument("--tg256", action="store_true",
@@ -167,8 +169,9 @@ def run_ours(args):
     dev = local
     n = args.n
     N = tuple(int(x) for x in args.grid.split(",")) if args.grid else (n, n, n)
-    uh0 = isotropic_field(N, k0=K0, energy=0.5, seed=0, dtype=np.complex64)
-    ctx = Context(N, nu=NU, precision="single", device=dev)
+    dbl = args.precision == "double"
+    uh0 = isotropic_field(N, k0=K0, energy=0.5, seed=0, dtype=np.complex128 if dbl else np.complex64)
+    ctx = Context(N, nu=NU, precision=args.precision, device=dev)
     ctx.set_forcing(EPS, KF)
     ctx.set_cfl(CFL)
     ctx.set_state(uh0)
@@ -203,7 +206,7 @@ def run_ours(args):
     value = ws * args.steps / (ms_max / 1e3)
 
     # per-kernel roofline
-    kb = kernel_bytes(N)
+    kb = kernel_bytes(N, csz=16 if dbl else 8)
     peak, peak_src = peaks()
     kernels = {}
     for i, name in enumerate(KERNEL_NAMES):
@@ -217,7 +220,7 @@ def run_ours(args):
     try:
         with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
             tr = json.load(f)
-        if str(n) in tr and dom in tr[str(n)]:
+        if str(n) in tr and dom in tr[str(n)] and not dbl and not args.grid:
             traffic = tr[str(n)][dom]
     except Exception:
         pass
@@ -239,10 +242,11 @@ def run_ours(args):
 
     out = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64" if dbl else "f32",
            "data": "synthetic (seeded spectrum, generated on the host; no dataset)",
-           "config": {"workload": WORKLOAD, "grid": list(N), "precision": "single (FP32 transforms, FP64 RK4 "
-                      "accumulators and reductions)", "l2": "inputs larger than L2 (1.6 GB state), no flush",
+           "config": {"workload": WORKLOAD if not dbl else WORKLOAD.replace("FP32", "FP64"), "grid": list(N),
+                      "precision": "double (everything FP64)" if dbl else "single (FP32 transforms, compensated "
+                      "FP32 RK4 accumulators, FP64 reductions)", "l2": "inputs larger than L2 (1.6 GB state), no flush",
                       "parallelism": "replicas" if ws > 1 else "single GPU",
                       "timing": "CUDA events on the solver stream; per-kernel events in the same region"},
            "roofline": roofline, "kernels": kernels, "gpu_launches": launches, "clocks": clocks,
@@ -252,8 +256,9 @@ def run_ours(args):
     if not args.no_e2e:
         ke = max(3, min(args.steps, 10))
         shape = ctx.spec_shape
-        hin = torch.empty(shape, dtype=torch.complex64, pin_memory=True)
-        hout = torch.empty(shape, dtype=torch.complex64, pin_memory=True)
+        cdt = torch.complex128 if dbl else torch.complex64
+        hin = torch.empty(shape, dtype=cdt, pin_memory=True)
+        hout = torch.empty(shape, dtype=cdt, pin_memory=True)
         hin.numpy()[...] = uh0
         ctx.set_state(hin)
         ctx.rk4(0.0, 1)
@@ -269,7 +274,7 @@ def run_ours(args):
         tt = torch.tensor([te], device="cuda:%d" % dev)
         if ws > 1:
             torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        nbytes = int(np.prod(shape)) * 8
+        nbytes = int(np.prod(shape)) * (16 if dbl else 8)
         out["e2e"] = {"value": ws * ke / float(tt.item()), "unit": "steps/s", "h2d_bytes_per_step": nbytes,
                       "d2h_bytes_per_step": nbytes, "steps": ke,
                       "path": "Context.set_state(pinned host) + rk4 + get_state(pinned host) per step"}

@@ -219,7 +219,8 @@ int sdns_to_bf16(const float* a, void* b, int64_t count, void* stream);
  * scratch is one static device array of SDNS_NOALLOC_SCRATCH_BYTES that every
  * GPU loading the library keeps until the process exits; grids that need
  * more (about 64^3 in double, 64x64x128 in single precision is the limit)
- * are rejected with SDNS_EINVAL.  The first call on a device looks up the
+ * are rejected with SDNS_EINVAL, and so are the 3/2 rule and the SDNS_VV
+ * formulation.  The first call on a device looks up the
  * array's device address, so make that call before any stream capture.  All
  * calls share the array: calls that overlap on the GPU race and must be
  * serialised by the caller.  Errors are reported through sdns_last_error. */

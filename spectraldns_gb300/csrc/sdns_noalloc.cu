@@ -287,6 +287,8 @@ int sdns_compute_rhs_noalloc(const sdns_config* cfg, const void* u_hat, void* rh
     return na_fail(SDNS_EINVAL, "precision must be SDNS_SINGLE or SDNS_DOUBLE");
   if (cfg->dealias != SDNS_DEALIAS_23 && cfg->dealias != SDNS_DEALIAS_NONE)
     return na_fail(SDNS_EINVAL, "dealias must be SDNS_DEALIAS_23 or SDNS_DEALIAS_NONE");
+  if (cfg->formulation != SDNS_NS)
+    return na_fail(SDNS_EINVAL, "the allocation-free right-hand side is the velocity (SDNS_NS) formulation only");
   int prev = 0;
   if (cudaGetDevice(&prev) != cudaSuccess) { cudaGetLastError(); return na_fail(SDNS_ECUDA, "no CUDA device"); }
   if (cfg->device != prev && cudaSetDevice(cfg->device) != cudaSuccess) {

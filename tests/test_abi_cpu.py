@@ -45,3 +45,19 @@ def test_abi_version_and_error_without_gpu():
     h = C.c_void_p()
     assert L.sdns_create(C.byref(cfg), C.byref(h)) == _lib.SDNS_EINVAL
     assert b"powers of two" in L.sdns_last_error()
+
+
+def test_noalloc_rejects_unsupported_configs_without_gpu():
+    """The allocation-free entry point checks its configuration before any CUDA call: the
+    3/2 rule and the velocity-vorticity formulation are rejected."""
+    import ctypes as C
+    from spectraldns_gb300 import _lib
+    L = _lib.lib()
+    for dealias, form in ((_lib.SDNS_DEALIAS_32, _lib.SDNS_NS), (_lib.SDNS_DEALIAS_23, _lib.SDNS_VV)):
+        cfg = _lib.sdns_config()
+        cfg.n[:] = (16, 16, 16)
+        cfg.L[:] = (1.0, 1.0, 1.0)
+        cfg.dealias = dealias
+        cfg.formulation = form
+        buf = (C.c_byte * 16)()
+        assert L.sdns_compute_rhs_noalloc(C.byref(cfg), buf, buf, None) == _lib.SDNS_EINVAL
