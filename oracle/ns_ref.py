@@ -50,9 +50,12 @@ constant-power low-wavenumber forcing (a ``Source`` recomputed at the start
 of every RK4 step) and the CFL time step.
 
 Parity pins: the Taylor-Green known answers ``k=0.124953117517`` and
-``w=0.375249930801`` (``tests/TG.py:125-126``, ``spectralDNS3D_short.py:113``)
-and state fixtures produced by running ``spectralDNS3D_short.py`` itself
-(``tests/golden/make_golden.py``).
+``w=0.375249930801`` (``tests/TG.py:125-126``, ``spectralDNS3D_short.py:113``);
+state fixtures produced by running ``spectralDNS3D_short.py`` itself
+(``tests/golden/make_golden.py``); and the reference's own compiled Cython
+kernels ``cross1``, ``cross2``, ``add_pressure_diffusion_NS``, ``RK4``,
+``ForwardEuler`` and ``AB2`` (``oracle/build_ref_cython.py``,
+``tests/test_oracle_ref_cython.py``).
 """
 from __future__ import annotations
 
