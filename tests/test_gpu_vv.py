@@ -104,3 +104,22 @@ def test_vv_solver_api(built_lib, mesh, integrator, ntol):
     solve(solver, context)
     div = solver.get_divergence(**context)
     assert np.max(np.abs(div)) < 1e-10
+
+
+@pytest.mark.parametrize("prec", ["double", "single"])
+def test_vv_cfl_step(built_lib, prec):
+    """VV with the CFL time step: the z sweep's velocity fields are i K x w / K^2, so dt comes
+    from the velocity of the vorticity state, as for NS."""
+    N, L = (32, 32, 32), (2 * np.pi,) * 3
+    g = Grid(N, L, nu=0.01)
+    wh = vorticity(g, 12) * 20
+    c = vv_ctx(N, L, prec, nu=0.01)
+    c.set_state(wh.astype(c.complex))
+    c.set_cfl(0.5)
+    c.rk4(0.0, 1)
+    d = c.diagnostics()
+    rate = g.cfl_rate(g.velocity_of_vorticity(wh))
+    dt = 0.5 / rate
+    assert abs(d["last_dt"] - dt) < (1e-12 if prec == "double" else 1e-5) * dt
+    ref = g.rk4_step(wh, dt, vv=True)
+    assert relerr(c.get_state(), ref) < (1e-11 if prec == "double" else 2e-5)
