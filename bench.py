@@ -231,8 +231,8 @@ def run_ours(args):
                 "step_achieved_gbs": step_bytes / (ms / args.steps * 1e-3) / 1e9}
     roofline["step_frac"] = roofline["step_achieved_gbs"] / peak
     # the same step against the full-spectral-array byte model 4 (27 + 9a) F per step,
-    # F = 8 N0 N1 (N2/2+1): a = 2 for 16-byte accumulators (this build's compensated FP32 S, A),
-    # a = 1 for 8-byte ones; this build stores only the kept modes and moves fewer bytes
+    # F = 8 N0 N1 (N2/2+1): a = 2 for 16-byte accumulators (the library's compensated FP32 S, A),
+    # a = 1 for 8-byte ones; the library stores only the kept modes and moves fewer bytes
     F = 8.0 * N[0] * N[1] * (N[2] // 2 + 1)
     t_step = ms / args.steps * 1e-3
     roofline["full_array_model"] = {
