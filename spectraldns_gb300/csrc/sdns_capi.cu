@@ -1104,6 +1104,7 @@ int sdns_set_state(sdns_ctx* c, const void* u_hat, int where) {
   if (!u_hat) return fail(SDNS_EINVAL, "null u_hat");
   if (c->pad32) {
     if ((e = copy_in(c, c->U32, u_hat, 3 * c->nfull1 * (long long)c->csz, where))) return e;
+    CK(cudaMemsetAsync(c->sc + SC_FLAG, 0, 8, c->st));
     CK(cudaStreamSynchronize(c->st));
     c->has_state = true;
     return SDNS_OK;
@@ -1112,6 +1113,7 @@ int sdns_set_state(sdns_ctx* c, const void* u_hat, int where) {
   if ((e = copy_in(c, c->stage, u_hat, 3 * c->nfull1 * (long long)c->csz, where))) return e;
   Geo g = geo(c);
   CK(cudaMemsetAsync(c->flag, 0, 4, c->st));
+  CK(cudaMemsetAsync(c->sc + SC_FLAG, 0, 8, c->st));  // a new state clears an earlier non-finite report
   if (c->dbl) {
     k_gather<double2><<<nblocks(3 * c->ncomp1), 256, 0, c->st>>>((const double2*)c->stage, (double2*)c->Y, c->S, g, c->ncomp1);
     k_outside<double2><<<nblocks(3 * c->nfull1), 256, 0, c->st>>>((const double2*)c->stage, g, c->flag);
