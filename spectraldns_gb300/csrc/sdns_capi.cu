@@ -1166,7 +1166,7 @@ int sdns_set_source(sdns_ctx* c, const void* source, int where) {
   if (c->pad32) {  // the padded right-hand side reads the caller-layout source
     if (!c->src_full && (e = dalloc(c, &c->src_full, 3 * c->nfull1 * (long long)c->csz))) return e;
     if ((e = copy_in(c, c->src_full, source, 3 * c->nfull1 * (long long)c->csz, where))) return e;
-    CK(cudaStreamSynchronize(c->st));
+    if (where == SDNS_HOST) CK(cudaStreamSynchronize(c->st));
     return SDNS_OK;
   }
   if (!c->src && (e = dalloc(c, &c->src, 3 * c->ncomp1 * 16))) return e;
@@ -1178,7 +1178,8 @@ int sdns_set_source(sdns_ctx* c, const void* source, int where) {
   else
     k_gather<float2><<<nblocks(3 * c->ncomp1), 256, 0, c->st>>>((const float2*)c->src_full, nullptr, c->src, g, c->ncomp1);
   CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(c->st));
+  // a host source may be released on return; a device source is ordered on the stream
+  if (where == SDNS_HOST) CK(cudaStreamSynchronize(c->st));
   return SDNS_OK;
 }
 

@@ -65,6 +65,11 @@ class Context:
         check(self._L.sdns_create(C.byref(cfg), C.byref(h)))
         self._h = h
         self._keep = []
+        # ordered = True: the caller launches everything that produces or reads the device
+        # tensors it passes on the context stream (e.g. under torch.cuda.stream of
+        # torch.cuda.ExternalStream(stream_handle())), so calls skip the host synchronisations
+        # that otherwise order torch's stream and the context stream around them
+        self.ordered = False
 
     # -- plumbing -----------------------------------------------------------
     def close(self):
@@ -89,7 +94,8 @@ class Context:
                     t = t.to(_torch_dtype(dtype))
                 if tuple(t.shape) != tuple(shape):
                     t = t.reshape(shape)
-                torch.cuda.current_stream(t.device).synchronize()
+                if not self.ordered:
+                    torch.cuda.current_stream(t.device).synchronize()
                 return t.data_ptr(), _lib.SDNS_DEVICE, t
             a = a.numpy()
         arr = np.ascontiguousarray(a, dtype=dtype)
@@ -106,7 +112,8 @@ class Context:
             if out.is_cuda:
                 if not out.is_contiguous() or out.dtype != _torch_dtype(dtype):
                     raise ValueError("device output must be a contiguous %s tensor" % dtype)
-                torch.cuda.current_stream(out.device).synchronize()
+                if not self.ordered:
+                    torch.cuda.current_stream(out.device).synchronize()
                 return out.data_ptr(), _lib.SDNS_DEVICE, out, None
             if out.is_contiguous() and out.dtype == _torch_dtype(dtype):
                 return out.data_ptr(), _lib.SDNS_HOST, out, None
@@ -118,7 +125,7 @@ class Context:
         return tmp.ctypes.data, _lib.SDNS_HOST, tmp, out
 
     def _finish(self, arr, writeback, where):
-        if where == _lib.SDNS_DEVICE:
+        if where == _lib.SDNS_DEVICE and not self.ordered:
             check(self._L.sdns_synchronize(self._h))
         if writeback is not None:
             if _is_torch(writeback):
@@ -277,7 +284,8 @@ class Context:
         other call of the context that takes device tensors.
         """
         n = len(terms)
-        torch.cuda.current_stream(out.device).synchronize()
+        if not self.ordered:
+            torch.cuda.current_stream(out.device).synchronize()
         if n != len(coefs) or n > _lib.SDNS_LINCOMB_MAX:
             raise ValueError("at most %d terms, one coefficient each" % _lib.SDNS_LINCOMB_MAX)
         po = self._dev_vec(out, "out")
@@ -290,7 +298,8 @@ class Context:
     def error_norm(self, err, u0, u1, atol, rtol):
         """float64 [sum_k |err/sc|^2 for k = 0, 1, 2], sc = atol + max(|u0|, |u1|) rtol."""
         sums = (C.c_double * 3)()
-        torch.cuda.current_stream(err.device).synchronize()
+        if not self.ordered:
+            torch.cuda.current_stream(err.device).synchronize()
         check(self._L.sdns_error_norm(self._h, C.c_void_p(self._dev_vec(err, "err")),
                                       C.c_void_p(self._dev_vec(u0, "u0")), C.c_void_p(self._dev_vec(u1, "u1")),
                                       float(atol), float(rtol), sums))

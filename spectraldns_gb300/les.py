@@ -244,6 +244,9 @@ class LES:
         self.tauhat = torch.empty((6,) + self.ctx.spec_shape[1:], dtype=torch.complex64, device=self.dev)
         self.force = torch.empty(self.ctx.spec_shape, dtype=torch.complex64, device=self.dev)
         self.L = _lib.lib()
+        # the closure's kernels run on the context stream, so one LES step needs no host
+        # synchronisation between the network, the transforms and the RK4 step
+        self.stream = torch.cuda.ExternalStream(self.ctx.stream_handle(), device=self.dev)
 
     def set_velocity_phys(self, ubar):
         """Start from a filtered velocity, truncated to the modes the LES keeps (2/3 rule)."""
@@ -251,18 +254,23 @@ class LES:
 
     def closure_source(self):
         nm = self.norms
-        self.ctx.get_state(out=self.uhat)
-        g = self.feat.gradients(self.uhat)
-        x = self.feat.pack(g.reshape(9, -1), nm["fmu"], nm["fisd"])
-        y = self.net.forward(x)
-        check(self.L.sdns_les_unpack(_p(y), CPAD_OUT, NOUT, self.feat.P, _p(nm["tmu"]), _p(nm["tsd"]), _p(self.tau),
-                                     _stream()))
-        self.ctx.forward(self.tau[0:3], out=self.tauhat[0:3])
-        self.ctx.forward(self.tau[3:6], out=self.tauhat[3:6])
-        check(self.L.sdns_les_sgs_force(_p(self.tauhat), _p(self.force), _lib.SDNS_SINGLE, _ivec(self.ctx.N),
-                                        _dvec(self.ctx.L), self.scale, _stream()))
-        torch.cuda.synchronize()
-        self.ctx.set_source(self.force)
+        self.stream.wait_stream(torch.cuda.current_stream(self.dev))  # weights and norms come from torch's stream
+        self.ctx.ordered = True
+        try:
+            with torch.cuda.stream(self.stream):
+                self.ctx.get_state(out=self.uhat)
+                g = self.feat.gradients(self.uhat)
+                x = self.feat.pack(g.reshape(9, -1), nm["fmu"], nm["fisd"])
+                y = self.net.forward(x)
+                check(self.L.sdns_les_unpack(_p(y), CPAD_OUT, NOUT, self.feat.P, _p(nm["tmu"]), _p(nm["tsd"]),
+                                             _p(self.tau), _stream()))
+                self.ctx.forward(self.tau[0:3], out=self.tauhat[0:3])
+                self.ctx.forward(self.tau[3:6], out=self.tauhat[3:6])
+                check(self.L.sdns_les_sgs_force(_p(self.tauhat), _p(self.force), _lib.SDNS_SINGLE,
+                                                _ivec(self.ctx.N), _dvec(self.ctx.L), self.scale, _stream()))
+                self.ctx.set_source(self.force)
+        finally:
+            self.ctx.ordered = False
 
     def step(self):
         if self.net is not None:
@@ -469,6 +477,26 @@ def run_experiment(out_json, n_dns=512, ratio=8, steps=2000, every=10, iters=300
     return out
 
 
+def evaluate_model(out_json, model, n_dns=512, ratio=8, steps=2000, every=10, train_frac=0.75, log=print):
+    """The held-out evaluation of run_experiment with saved weights: the DNS trajectory is
+    deterministic, so it is regenerated, and the LES with and without the closure is run and
+    timed again on the snapshots after the training window."""
+    data = harvest(n_dns, ratio, steps, every, log=log)
+    nc = n_dns // ratio
+    ntrain = int(data["ubar"].shape[0] * train_frac)
+    net, nm, scale = load_model(model, (nc,) * 3)
+    ev = evaluate(data, net, nm, ntrain, nc, log=log, scale=scale)
+    dns_s_per_time = data["dns_gpu_ms"] / 1e3 / max(data["dns_time"], 1e-30)
+    out = {"n_dns": n_dns, "n_les": nc, "ratio": ratio, "dns_steps": steps, "snapshots": int(data["ubar"].shape[0]),
+           "train_snapshots": ntrain, "model": os.path.basename(model), "scale": scale,
+           "dns_gpu_s_per_sim_time": dns_s_per_time, "evaluation": ev,
+           "speedup_gpu_seconds": dns_s_per_time / ev["closure"]["s_per_sim_time"],
+           "speedup_no_closure": dns_s_per_time / ev["no_closure"]["s_per_sim_time"]}
+    with open(out_json, "w") as f:
+        json.dump(out, f, indent=1)
+    return out
+
+
 def save_model(path, net, nm, scale=1.0):
     np.savez(path, w=net.state_dict()["w"], scale=np.float64(scale), **{k: v.cpu().numpy() for k, v in nm.items()})
 
@@ -493,7 +521,12 @@ if __name__ == "__main__":
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--every", type=int, default=10)
     ap.add_argument("--iters", type=int, default=3000)
+    ap.add_argument("--evaluate", default=None, metavar="MODEL",
+                    help="only re-run the held-out evaluation with these saved weights")
     a = ap.parse_args()
-    r = run_experiment(a.out, a.n, a.ratio, a.steps, a.every, a.iters, log=lambda s: print(s, flush=True))
+    if a.evaluate:
+        r = evaluate_model(a.out, a.evaluate, a.n, a.ratio, a.steps, a.every, log=lambda s: print(s, flush=True))
+    else:
+        r = run_experiment(a.out, a.n, a.ratio, a.steps, a.every, a.iters, log=lambda s: print(s, flush=True))
     print(json.dumps({k: v for k, v in r.items() if k != "evaluation"}))
     print(json.dumps(r["evaluation"]))
