@@ -295,6 +295,23 @@ def cross2(c, a, b):
     return c
 
 
+def Cross(c, a, b, work, T):
+    """c = F(a x b) for physical vectors a, b (NS.py:131-136); the transform runs on the GPU."""
+    ab = work[(a, 0, False)] if isinstance(work, _Work) else np.empty_like(a)
+    ab = cross1(ab, a, b)
+    return T.forward(ab, c)
+
+
+def standard_convection(rhs, u_dealias, U_hat, work, Tp, K):
+    """The 'Standard' convection form (NS.py:138-145) is not provided by the GB300 backend."""
+    raise NotImplementedError("the GB300 backend implements the Vortex convection form")
+
+
+def divergence_convection(rhs, u_dealias, work, Tp, K, add=False):
+    """The 'Divergence' convection form (NS.py:147-162) is not provided by the GB300 backend."""
+    raise NotImplementedError("the GB300 backend implements the Vortex convection form")
+
+
 def getConvection(convection):
     """The convection term is fused into ComputeRHS on the GPU (Vortex form only)."""
     if convection != "Vortex":

@@ -129,3 +129,18 @@ def test_restart_from_checkpoint(tmp_path, monkeypatch, precision, integrator):
     restarted, nrest = run(restart=True)
     assert nrest == nfull and nfull in (10, 11)
     assert np.array_equal(restarted, full)
+
+
+def test_cross_helper():
+    """NS.Cross (NS.py:131-136): the forward transform of a x b, on the GPU transform."""
+    from spectraldns_gb300 import get_solver
+    solver = get_solver(parse_args=["--M", "4", "4", "4", "NS"])
+    context = solver.get_context()
+    g = Grid((16, 16, 16))
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal((3, 16, 16, 16))
+    b = rng.standard_normal((3, 16, 16, 16))
+    c = np.zeros(context.U_hat.shape, dtype=context.U_hat.dtype)
+    c = solver.Cross(c, a, b, context.work, context.VT)
+    ref = g.forward(g.cross(a, b))
+    assert np.max(np.abs(c - ref)) < 1e-12 * np.max(np.abs(ref))
