@@ -160,6 +160,26 @@ class NSFile(HDF5File):
                 _fresh(val[0], context.get("gpu"))
 
 
+class Field(np.ndarray):
+    """A host array of the context that can transform itself, the part of shenfun's
+    Array / Function the demos use (demo/TG.py:100 calls ``U.forward(U_hat)``): a physical
+    field's ``forward`` and a spectral field's ``backward`` run on the GPU through its space."""
+
+    def __new__(cls, space, spectral, dtype):
+        obj = np.zeros(space.shape(spectral), dtype=dtype).view(cls)
+        obj.space = space
+        return obj
+
+    def __array_finalize__(self, obj):
+        self.space = getattr(obj, "space", None)
+
+    def forward(self, output_array=None):
+        return self.space.forward(np.asarray(self), output_array)
+
+    def backward(self, output_array=None):
+        return self.space.backward(np.asarray(self), output_array)
+
+
 class _Work(dict):
     """Cached work arrays keyed like shenfun's CachedArrayDict: (array, index, zero)."""
 
@@ -210,14 +230,14 @@ def get_context(formulation="NS"):
     for i in range(3):
         K_over_K2[i] = K[i] / K2n
     del K2n, x, ki
-    U = np.zeros(VT.shape(False), dtype=float_)
-    U_hat = np.zeros(VT.shape(True), dtype=complex_)
-    P = np.zeros(T.shape(False), dtype=float_)
-    P_hat = np.zeros(T.shape(True), dtype=complex_)
+    U = Field(VT, False, float_)
+    U_hat = Field(VT, True, complex_)
+    P = Field(T, False, float_)
+    P_hat = Field(T, True, complex_)
     u_dealias = U
     u = U_hat
     dU = np.zeros(VT.shape(True), dtype=complex_)
-    curl = np.zeros(VT.shape(False), dtype=float_)
+    curl = Field(VT, False, float_)
     Source = np.zeros(VT.shape(True), dtype=complex_)
     work = _Work()
     hdf5file = NSFile(params.solver, checkpoint={"space": VT, "data": {"0": {"U": [U_hat]}}},

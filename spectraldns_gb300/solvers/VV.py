@@ -18,7 +18,7 @@ from __future__ import annotations
 import numpy as np
 
 from .NS import *  # noqa: F401,F403
-from .NS import _fresh, _push_source, get_context as NS_context, params  # noqa: F401
+from .NS import Field, _fresh, _push_source, get_context as NS_context, params  # noqa: F401
 from ..h5io import HDF5File
 
 
@@ -26,7 +26,7 @@ def get_context():
     """Context of the VV solver (VV.py:23-38): NS's arrays without P, P_hat; W_hat is the state."""
     c = NS_context(formulation="VV")
     del c["P"], c["P_hat"]
-    c.W_hat = np.zeros_like(c.U_hat)
+    c.W_hat = Field(c.VT, True, c.complex)
     c.u = c.W_hat
     c.hdf5file = VVFile(params.solver, checkpoint={"space": c.VT, "data": {"0": {"curl": [c.W_hat]}}},
                         results={"space": c.VT, "data": {"U": [c.U], "curl": [c.curl]}})
