@@ -58,6 +58,9 @@ def parse():
                    help="precision of the main workload (profiling the FP64 kernels); the headline is single")
     p.add_argument("--grid", default=None,
                    help="N0,N1,N2: run the workload on this (small, profiling) grid instead of --n cubed")
+    p.add_argument("--decay1024-steps", type=int, default=0, dest="decay1024_steps",
+                   help="only run the 1024^3 decaying-turbulence case for this many RK4 steps with FP64 energy and "
+                        "dissipation every step, and print its energy budget")
     p.add_argument("--tg256", action="store_true",
                    help="only run the 256^3 Taylor-Green FP32-vs-FP64 comparison (1000 steps) and print it")
     return p.parse_args()
@@ -459,6 +462,46 @@ def cufft_compare(dev, ws, N, ours_steps_per_s, steps=5, dt=1e-3):
                     "projection, diffusion, classic RK4 in FP32, fixed dt %g" % dt}
 
 
+def decay_1024_run(dev, steps=500):
+    """The 1024^3 decaying-turbulence case run to completion: FP64 kinetic energy E and dissipation
+    eps every step.  The dealiased u x w term conserves energy, so E(0) - E(t) must equal the time
+    integral of eps (trapezoid rule over the CFL steps); the relative residual of that budget, the
+    divergence and the final state are reported."""
+    from spectraldns_gb300.gpu import Context
+    from spectraldns_gb300.init import isotropic_field
+    N = (1024,) * 3
+    uh = isotropic_field(N, k0=6.0, energy=0.5, seed=0, dtype=np.complex64)
+    c = Context(N, nu=4e-4, precision="single", device=dev)
+    c.set_cfl(CFL)
+    c.set_state(uh)
+    del uh
+    E, D, T = [], [], []
+    d = c.diagnostics()
+    E.append(d["energy"]); D.append(d["dissipation"]); T.append(d["time"])
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        c.rk4(0.0, 1)
+        d = c.diagnostics()
+        E.append(d["energy"]); D.append(d["dissipation"]); T.append(d["time"])
+    wall = time.perf_counter() - t0
+    E, D, T = np.array(E), np.array(D), np.array(T)
+    lost = E[0] - E[-1]
+    integral = float(np.sum(0.5 * (D[1:] + D[:-1]) * np.diff(T)))
+    res = {"workload": "decaying isotropic turbulence 1024^3 FP32 (seeded k^4 exp(-2(k/6)^2), E=0.5, nu=4e-4, "
+                       "no forcing, RK4 CFL 0.5, FP64 energy and dissipation every step)",
+           "steps": steps, "wall_s_with_diagnostics": wall, "steps_per_s_with_diagnostics": steps / wall,
+           "time": float(T[-1]), "energy_initial": float(E[0]), "energy_final": float(E[-1]),
+           "dissipation_initial": float(D[0]), "dissipation_final": float(D[-1]),
+           "dissipation_max": float(D.max()), "energy_monotone": bool(np.all(np.diff(E) <= 1e-12 * E[0])),
+           "energy_lost": float(lost), "dissipation_integral": integral,
+           "budget_rel_residual": float(abs(lost - integral) / max(lost, 1e-300)),
+           "divergence_final": d["divergence"], "cfl_rate_final": d["cfl_rate"],
+           "energy_every_50": E[::50].tolist(), "dissipation_every_50": D[::50].tolist(), "time_every_50": T[::50].tolist(),
+           "hbm_bytes": c.memory_bytes()}
+    c.close()
+    return res
+
+
 def pad32_line(dev, ws, n=256, steps=10):
     """RK4 steps/s of the same seeded isotropic field at n^3 FP32 (fixed dt) with the 3/2 rule (padded
     3n/2 transforms, generic mixed-radix kernels) and with the 2/3 rule (fused sweeps), for the cost of
@@ -611,6 +654,8 @@ def main():
     args = parse()
     if args.tg256:
         print(json.dumps(tg256(int(os.environ.get("LOCAL_RANK", "0")))), flush=True)
+    elif args.decay1024_steps > 0:
+        print(json.dumps(decay_1024_run(int(os.environ.get("LOCAL_RANK", "0")), args.decay1024_steps)), flush=True)
     elif args.impl == "reference":
         run_reference(args)
     else:
