@@ -120,6 +120,28 @@ def test_tg_fp32_drift(built_lib):
     assert abs(e - g.kinetic_energy(ref)) / g.kinetic_energy(ref) < 1e-5
 
 
+def test_tg_config0_fp64_100_steps(built_lib):
+    """The Taylor-Green case of the reference's CPU demo run (32^3, float64, nu = 0.000625,
+    dt = 0.01, 100 RK4 steps, 2/3 rule): state against the float64 oracle to 1e-11 relative, and
+    energy, enstrophy and dissipation every 10 steps to 1e-12 relative."""
+    N = (32, 32, 32)
+    g = Grid(N)
+    ref = g.forward(taylor_green(g))
+    c = ctx(N, (2 * np.pi,) * 3, "double")
+    c.set_state(ref)
+    for _ in range(10):
+        for _ in range(10):
+            ref = g.rk4_step(ref, 0.01)
+        c.rk4(0.01, 10)
+        d = c.diagnostics()
+        k, w = g.kinetic_energy(ref), g.enstrophy(ref)
+        assert abs(d["energy"] - k) < 1e-12 * k
+        assert abs(d["enstrophy"] - w) < 1e-12 * w
+        assert abs(d["dissipation"] - g.dissipation(ref)) < 1e-12 * g.dissipation(ref)
+    assert relerr(c.get_state(), ref) < 1e-11
+    assert abs(d["time"] - 1.0) < 1e-12
+
+
 def test_diagnostics_and_spectrum(built_lib):
     N = (32, 32, 32)
     g = Grid(N)
