@@ -66,6 +66,16 @@ def parse():
     return p.parse_args()
 
 
+def max_over_ranks(x, ws, device):
+    """The largest of the ranks' values (the job's time is its slowest rank's); x itself when ws == 1.
+    device: where the reduction tensor lives ("cuda:<i>" for NCCL, "cpu" for gloo)."""
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    if ws > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -202,10 +212,7 @@ def run_ours(args):
     ctx.set_timing(False)
     diag = ctx.diagnostics()
     dns_s_per_sim_time = (ms / 1e3) / max(diag["time"] - t_start, 1e-30)
-    t_ms = torch.tensor([ms], device="cuda:%d" % dev)
-    if ws > 1:
-        torch.distributed.all_reduce(t_ms, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t_ms.item())
+    ms_max = max_over_ranks(ms, ws, "cuda:%d" % dev)
     value = ws * args.steps / (ms_max / 1e3)
 
     # per-kernel roofline
@@ -274,11 +281,9 @@ def run_ours(args):
             ctx.rk4(0.0, 1)
             ctx.get_state(hout)      # device -> host: the step's result (synchronous)
         te = time.perf_counter() - t0
-        tt = torch.tensor([te], device="cuda:%d" % dev)
-        if ws > 1:
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        te_max = max_over_ranks(te, ws, "cuda:%d" % dev)
         nbytes = int(np.prod(shape)) * (16 if dbl else 8)
-        out["e2e"] = {"value": ws * ke / float(tt.item()), "unit": "steps/s", "h2d_bytes_per_step": nbytes,
+        out["e2e"] = {"value": ws * ke / te_max, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
                       "d2h_bytes_per_step": nbytes, "steps": ke,
                       "path": "Context.set_state(pinned host) + rk4 + get_state(pinned host) per step"}
     ctx.close()
