@@ -174,3 +174,22 @@ def test_three_halves_rule_is_alias_free():
     assert np.abs(nl - exs).max() < 1e-14 * np.abs(exs).max()
     # the 2/3 rule on the same (unpadded) grid is a different, truncating approximation
     assert np.abs(Grid((16, 16, 16))._nonlinear(a, b) - exs).max() > 1e-3 * np.abs(exs).max()
+
+
+def test_three_halves_rule_vv_is_curl_of_ns():
+    """With the 3/2 rule as well, the velocity-vorticity trajectory of a zero-mean solenoidal field
+    is the curl of the velocity trajectory (the padded nonlinear terms agree: i K x P(nl) = i K x nl)."""
+    g = Grid((16, 16, 16), dealias="3/2-rule")
+    uh = g.forward(taylor_green(g))
+    rng = np.random.default_rng(3)
+    pert = g.forward(rng.standard_normal((3,) + g.N)) * g.mask * 0.05
+    P = sum(g.K[i] * pert[i] for i in range(3))
+    for i in range(3):
+        pert[i] -= P * g.K_over_K2[i]
+    pert[:, 0, 0, 0] = 0  # the VV form carries no mean flow (i K x w / K^2 is 0 at K = 0)
+    uh = uh + pert
+    wh = g.curl_hat(uh)
+    for _ in range(5):
+        uh = g.rk4_step(uh, 0.01)
+        wh = g.rk4_step(wh, 0.01, vv=True)
+    assert np.max(np.abs(wh - g.curl_hat(uh))) < 1e-13 * np.max(np.abs(wh))
