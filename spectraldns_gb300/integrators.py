@@ -49,9 +49,9 @@ class DeviceIntegrator:
     ``step(dt, tstep)`` returns ``(dt_next, dt_taken)`` like the reference's
     integrator closures.  ``u`` is the current solution (a torch CUDA tensor
     in the layout of U_hat); ``step`` returns after the context stream has
-    finished it, so torch may read it at once.  ``callback(fu0)`` is called with the first
-    stage's right-hand side of every embedded-RK attempt (the reference sets
-    ``context.fu0`` and calls ``additional_callback``, :73-75).
+    finished it, so torch may read it at once.  ``callback(fu0)`` is called
+    with the first stage's right-hand side of every embedded-RK attempt (the
+    reference sets ``context.fu0`` and calls ``additional_callback``, :73-75).
     """
 
     def __init__(self, ctx, method, tol=1e-6, callback=None):
