@@ -131,3 +131,27 @@ def test_solver_module_names_match_reference(name):
         from spectraldns_gb300 import config, get_solver
         sol = get_solver(parse_args=["--M", "4", "4", "4", "VV"])
         assert sol is mod and config.params.solver == "VV"
+
+
+def test_lazy_checkpoint_refreshes_host_state(tmp_path):
+    """With --gpu_sync lazy the host U_hat lags the GPU state: the checkpoint pulls the state
+    first (NSFile.refresh), then writes it."""
+    from spectraldns_gb300 import config
+    from spectraldns_gb300.solvers.NS import NSFile
+
+    class FakeGPU:
+        host_stale = True
+
+        def __init__(self, arr):
+            self.host_U_hat = arr
+
+        def get_state(self, out):
+            out[...] = 7.0
+            return out
+
+    U_hat = np.zeros((3, 4, 4, 3), complex)
+    gpu = FakeGPU(U_hat)
+    f = NSFile(str(tmp_path / "lazy"), checkpoint={"data": {"0": {"U": [U_hat]}}})
+    f.write_checkpoint(config.Params(t=0.1, tstep=3), gpu=gpu)
+    d = np.load(str(tmp_path / "lazy_c.npz"))
+    assert np.all(d["U/3D/0"] == 7.0) and not gpu.host_stale
