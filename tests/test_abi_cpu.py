@@ -61,3 +61,26 @@ def test_noalloc_rejects_unsupported_configs_without_gpu():
         cfg.formulation = form
         buf = (C.c_byte * 16)()
         assert L.sdns_compute_rhs_noalloc(C.byref(cfg), buf, buf, None) == _lib.SDNS_EINVAL
+
+
+def test_header_is_c99_and_links():
+    """include/sdns_gb300.h is plain C: a C99 program compiles against it with -Wall -Werror,
+    links with libsdns_gb300.so and makes the calls that need no GPU (tests/c/abi_c99.c)."""
+    import shutil
+    import subprocess
+    import tempfile
+    from spectraldns_gb300 import build
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not available")
+    lib = build.build()
+    with tempfile.TemporaryDirectory() as tmp:
+        exe = os.path.join(tmp, "abi_c99")
+        cmd = [gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+               os.path.join(ROOT, "tests", "c", "abi_c99.c"), "-o", exe, "-L", os.path.dirname(lib),
+               "-l:" + os.path.basename(lib), "-Wl,-rpath," + os.path.dirname(lib)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+        assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+        assert "c99 caller ok" in r.stdout
