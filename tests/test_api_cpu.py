@@ -155,3 +155,25 @@ def test_lazy_checkpoint_refreshes_host_state(tmp_path):
     f.write_checkpoint(config.Params(t=0.1, tstep=3), gpu=gpu)
     d = np.load(str(tmp_path / "lazy_c.npz"))
     assert np.all(d["U/3D/0"] == 7.0) and not gpu.host_stale
+
+
+@pytest.mark.parametrize("kw", [{"precision": "half"}, {"dealias": "4/3-rule"}, {"formulation": "MHD"}])
+def test_context_rejects_unsupported_options(kw):
+    """Unsupported precision, dealiasing or formulation are refused before any CUDA call."""
+    from spectraldns_gb300.gpu import Context
+    with pytest.raises(ValueError):
+        Context((16, 16, 16), **kw)
+
+
+def test_unsupported_solver_settings_raise():
+    """The NS module refuses the convection forms and the unmasked 'None' rule it does not implement
+    (before creating a GPU context)."""
+    from spectraldns_gb300 import config, get_solver
+    sol = get_solver(parse_args=["--M", "4", "4", "4", "--convection", "Standard", "NS"])
+    with pytest.raises(ValueError):
+        sol.get_context()
+    sol = get_solver(parse_args=["--M", "4", "4", "4", "--dealias", "None", "--no-mask_nyquist", "NS"])
+    with pytest.raises(ValueError):
+        sol.get_context()
+    with pytest.raises(NotImplementedError):
+        sol.standard_convection(None, None, None, None, None, None)
